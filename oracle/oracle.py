@@ -1,0 +1,119 @@
+"""ctypes wrapper of the C oracle (vefem_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by the tests, the smoke check and the
+CPU-baseline leg of the benchmark, never by the product.  The shared object is
+built by ``oracle/build.sh`` into ``oracle/_build/`` (git-ignored).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SO = os.path.join(HERE, "_build", "libvefem_oracle.so")
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    if force or not os.path.exists(SO) or os.path.getmtime(SO) < os.path.getmtime(
+            os.path.join(HERE, "vefem_oracle.c")):
+        subprocess.check_call(["bash", os.path.join(HERE, "build.sh")])
+    return SO
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(SO)
+        P = ctypes.c_void_p
+        I = ctypes.c_int
+        L.ora_element_batch.argtypes = [P, P, I, I, P, P, P, P, I, I, P, P, P, I]
+        L.ora_assemble.argtypes = [P, P, I, I, P, P, P, P, I, P, P, P, P, I]
+        L.ora_edge_open.argtypes = [P, P, I, I, P, P, P, P, I, I, P, P, P]
+        L.ora_gp_probe.argtypes = [P, P, I, I, P, P, P, P, I, P]
+        L.ora_gauss_tables.argtypes = [P, P]
+        for f in (L.ora_element_batch, L.ora_assemble, L.ora_edge_open, L.ora_gp_probe):
+            f.restype = I
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def _prep(phys, conn, xyz, TL, EU):
+    ip = np.ascontiguousarray(phys.int_params(), dtype=np.int32)
+    dp = np.ascontiguousarray(phys.dbl_params(), dtype=np.float64)
+    conn = np.ascontiguousarray(conn, dtype=np.int32)
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    TL = np.ascontiguousarray(TL, dtype=np.float64)
+    EU = np.ascontiguousarray(EU if EU is not None and len(EU) else np.zeros(1), dtype=np.float64)
+    return ip, dp, conn, xyz, TL, EU
+
+
+def gauss_tables():
+    t = np.zeros((6, 9, 9))
+    w = np.zeros(9)
+    lib().ora_gauss_tables(_p(t), _p(w))
+    return t, w
+
+
+def element_outputs(phys, conn, xyz, TL, EU, e0=0, e1=None, jacobian=True, nthreads=0):
+    """Element residuals [n, 9, 6], FD Jacobians [n, 9, 6, 9, 6] (TEMP_A_f(inod,ieq,jnod,jeq))
+    and Ac columns [n, 9, 6, nex] for elements [e0, e1)."""
+    ip, dp, conn, xyz, TL, EU = _prep(phys, conn, xyz, TL, EU)
+    nel = conn.shape[1]
+    nn = xyz.shape[1]
+    e1 = nel if e1 is None else e1
+    n = e1 - e0
+    res = np.zeros((n, 9, 6))
+    jac = np.zeros((n, 9, 6, 9, 6)) if jacobian else None
+    ac = np.zeros((n, 9, 6, max(phys.nex, 1))) if jacobian else None
+    rc = lib().ora_element_batch(_p(ip), _p(dp), nel, nn, _p(conn), _p(xyz), _p(TL), _p(EU), e0,
+                                 e1, _p(res), _p(jac), _p(ac), nthreads)
+    assert rc == 0
+    return res, jac, (ac[..., :phys.nex] if ac is not None else None)
+
+
+def assemble(phys, conn, xyz, TL, EU, rowptr, colind, jacobian=True, nthreads=0, b=None,
+             vals=None):
+    """Global residual b and CSR values (ADD semantics onto the given arrays)."""
+    ip, dp, conn, xyz, TL, EU = _prep(phys, conn, xyz, TL, EU)
+    nel = conn.shape[1]
+    nn = xyz.shape[1]
+    N = rowptr.shape[0] - 1
+    b = np.zeros(N) if b is None else b
+    vals = np.zeros(colind.shape[0]) if vals is None else vals
+    rowptr = np.ascontiguousarray(rowptr, dtype=np.int64)
+    colind = np.ascontiguousarray(colind, dtype=np.int32)
+    rc = lib().ora_assemble(_p(ip), _p(dp), nel, nn, _p(conn), _p(xyz), _p(TL), _p(EU),
+                            1 if jacobian else 0, _p(rowptr), _p(colind), _p(b),
+                            _p(vals) if jacobian else None, nthreads)
+    if rc != 0:
+        raise RuntimeError("oracle assembly: element entry missing from the CSR pattern")
+    return b, vals
+
+
+def edge_open(phys, conn, xyz, TL, EU, iel, ied, jacobian=True):
+    ip, dp, conn, xyz, TL, EU = _prep(phys, conn, xyz, TL, EU)
+    res = np.zeros((9, 6))
+    jac = np.zeros((9, 6, 9, 6)) if jacobian else None
+    ac = np.zeros((9, 6, max(phys.nex, 1))) if jacobian else None
+    lib().ora_edge_open(_p(ip), _p(dp), conn.shape[1], xyz.shape[1], _p(conn), _p(xyz), _p(TL),
+                        _p(EU), int(iel), int(ied), _p(res), _p(jac), _p(ac))
+    return res, jac, (ac[..., :phys.nex] if ac is not None else None)
+
+
+def gp_probe(phys, conn, xyz, TL, EU, iel):
+    """Per-Gauss-point [Momentum x/y, Continuity, Con_EQ 11/12/22, tlsme, tlsic, tlsce, tdcs, WET]."""
+    ip, dp, conn, xyz, TL, EU = _prep(phys, conn, xyz, TL, EU)
+    out = np.zeros((9, 11))
+    lib().ora_gp_probe(_p(ip), _p(dp), conn.shape[1], xyz.shape[1], _p(conn), _p(xyz), _p(TL),
+                       _p(EU), int(iel), _p(out))
+    return out
