@@ -1,0 +1,159 @@
+/*
+ * vefem.h -- C ABI of the GB300 (sm_103a) element-assembly library for the
+ * viscoelastic flow-around-a-cylinder solver.
+ *
+ * It replaces the reference's bulk assembly call
+ *     call setEquationsBulk(Problem, FE, Mesh, Boundary, GaussInt, Sol, &
+ *                           basis_p, Flag_NR, Elem, LS)
+ * (Equations_mod.F90:21-55, called from assemblePetscObjects,
+ * Newton_Raphson_mod.F90:332) and, optionally, the outlet open-boundary edge
+ * terms (setEquationsEdge, Equations_mod.F90:317-554, called at
+ * Newton_Raphson_mod.F90:349).  Like VecSetValues/MatSetValues with
+ * ADD_VALUES (Storage_mod.F90:10-115) it ADDS the element residuals into the
+ * global residual b and the element Jacobians into the values array of a
+ * frozen AIJ (CSR) pattern, one element after another in element order, so
+ * the global sums are bit-for-bit those of the reference's sequential loop.
+ *
+ * All arrays use the reference's own (Fortran column-major) layouts, so a
+ * Fortran host passes its arrays through iso_c_binding without copies:
+ *   conn  : Mesh%Connectivity(Nel, 9)   -> conn[inod*nel + iel], 1-based ids
+ *   xyz   : Mesh%Xi_Mesh(Nnodes, 3)     -> xyz[j*nnodes + node]
+ *   TL    : Sol%TL(Nnodes, Neq=6)       -> TL[ieq*nnodes + node]
+ *           field order Ux, Uy, P, Txx(Sxx), Txy(Sxy), Tyy(Syy)
+ *   EU    : Sol%EU(Nex)                 (Nex = 1: the arclength parameter ArN)
+ *   b     : LS%b_f, length N = Nnodes*6 + Nex, row (gnode-1)*6 + ieq-1
+ *   vals  : the AIJ values array of LS%A_f (MatSeqAIJGetArray), CSR order
+ *
+ * Errors: every entry point returns an int status (0 = OK), mirroring
+ * PETSc's ierr; the library never exits.  vefem_last_error() gives text.
+ * One context is used by one host thread at a time.
+ */
+#ifndef VEFEM_H
+#define VEFEM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VEFEM_ABI_VERSION 1
+
+/* status codes */
+#define VEFEM_OK 0
+#define VEFEM_ERR_ARG 1          /* invalid argument or size */
+#define VEFEM_ERR_PATTERN 2      /* CSR pattern lacks an element entry or is not node-blocked */
+#define VEFEM_ERR_CUDA 3         /* CUDA runtime error (text in vefem_last_error) */
+#define VEFEM_ERR_NOMEM 4        /* host or device allocation failed */
+#define VEFEM_ERR_UNSUPPORTED 5  /* option not available in this build */
+
+/* constitutive models, in the order of setConEQ_T / setConEQ_SQRT
+ * (Constitutive_Models_mod.F90:31-49, Constitutive_Models_SQRT_mod.F90:66-84) */
+#define VEFEM_MODEL_L_PTT 0      /* Oldroyd-B is L-PTT with VeN = 0 */
+#define VEFEM_MODEL_M_L_PTT 1
+#define VEFEM_MODEL_E_PTT 2
+#define VEFEM_MODEL_M_E_PTT 3
+#define VEFEM_MODEL_FENE_CR 4
+#define VEFEM_MODEL_FENE_P 5
+#define VEFEM_MODEL_GIESEKUS 6
+
+/* stress formulation, Parameters_mod.F90:122 (Stress_Reform) */
+#define VEFEM_FORM_T 0           /* polymer stress T */
+#define VEFEM_FORM_SQRT 1        /* square-root conformation S, c = S.S */
+
+/* vefem_assemble flags */
+#define VEFEM_RESIDUAL 0x1       /* add the element residuals into b ('MNR' and 'NRP') */
+#define VEFEM_JAC_FD64 0x2       /* add the FP64 forward-difference Jacobian ('NRP'),
+                                    the reference algorithm of storeBulk, bit-exact */
+#define VEFEM_ZERO_FIRST 0x100   /* zero b (and vals when a Jacobian is requested) before
+                                    adding, like initializeLSObjects (Petsc_mod.F90:747-763) */
+#define VEFEM_OUTLET_EDGES 0x200 /* also add the outlet open-BC edge terms (openBC,
+                                    Residuals_mod.F90:599-624) of the mesh's outlet edges */
+#define VEFEM_TIMING 0x1000      /* record per-kernel CUDA-event times (vefem_last_timing) */
+
+/* Run-time form of the reference's compile-time physics parameters
+ * (Parameters_mod.F90:98-122).  With nex = 1 (arclength continuation in Wi)
+ * the Weissenberg number at every Gauss point is Wi0 * EU[0]
+ * (setContinuationParameter, Element_Calculations_mod.F90:577-601);
+ * with nex = 0 it is WiN.  dt is huge(1d0) for steady runs
+ * (Physical_mod.F90:345); fd_eps is the absolute FD step (1e-8,
+ * perturbVariableReal, Tools_mod.F90:831-840). */
+typedef struct vefem_params {
+    int32_t model;
+    int32_t form;
+    int32_t nex;                 /* 0 or 1 */
+    int32_t reserved;
+    double ReN, WiN, BvN, VeN, DfN, Wi0, dt, fd_eps;
+} vefem_params;
+
+typedef struct vefem_mesh {
+    int32_t nnodes;
+    int32_t nel;
+    const int32_t *conn;         /* [9 * nel], conn[inod*nel + iel], 1-based node ids */
+    const double *xyz;           /* [3 * nnodes], xyz[j*nnodes + node] (z unused in 2-D) */
+    int32_t n_outlet_edges;      /* outlet edges for VEFEM_OUTLET_EDGES (may be 0) */
+    const int32_t *outlet_edge_elem;  /* [n] 0-based element of each edge (edge_elements_rank - 1) */
+    const int32_t *outlet_edge_id;    /* [n] local edge id 1..4: eta=-1, xi=+1, eta=+1, xi=-1 */
+} vefem_mesh;
+
+typedef struct vefem_csr {
+    int64_t n;                   /* rows = cols = nnodes*6 + nex */
+    const int64_t *rowptr;       /* [n + 1], 0-based */
+    const int32_t *colind;       /* [rowptr[n]], sorted within each row */
+} vefem_csr;
+
+typedef struct vefem_ctx vefem_ctx;
+
+/* Build the device-side tables for one mesh and one frozen AIJ pattern:
+ * gather map, per-node residual contributor lists, per node-pair CSR block
+ * offsets and contributor lists (the deterministic element-ordered scatter),
+ * and the Gauss/basis tables.  Replaces the preallocation the reference does
+ * with zero element blocks (preAllocatePetsc, Petsc_mod.F90:629-743): the
+ * pattern must contain every element block, and, when nex = 1, the last
+ * column in every node row. */
+int vefem_create(const vefem_mesh *mesh, const vefem_csr *pattern, const vefem_params *params,
+                 vefem_ctx **out);
+
+/* Change the physics parameters (model, form, Wi, beta, ...); nex must not change. */
+int vefem_set_params(vefem_ctx *ctx, const vefem_params *params);
+
+/* One bulk assembly: setEquationsBulk with Flag_NR = 'MNR' (VEFEM_RESIDUAL)
+ * or 'NRP' (VEFEM_RESIDUAL | VEFEM_JAC_FD64).
+ * on_device = 0: TL, EU, b, vals are host pointers (copied in and out;
+ *                pinned memory gives full link speed);
+ * on_device = 1: they are device pointers (CUDA unified addressing).
+ * vals is double[nnz] and may be NULL when no Jacobian is requested.
+ * The call returns when the results are in b and vals. */
+int vefem_assemble(vefem_ctx *ctx, const double *TL, const double *EU, int flags, double *b,
+                   double *vals, int on_device);
+
+/* Per-kernel times (milliseconds, CUDA events on the context's stream) of the
+ * last vefem_assemble called with VEFEM_TIMING:
+ * t[0] element kernel, t[1] residual scatter, t[2] Jacobian scatter,
+ * t[3] edge kernel + scatter, t[4] host<->device copies.  n = entries wanted. */
+int vefem_last_timing(const vefem_ctx *ctx, float *t, int n);
+
+/* Number of kernels the library launched in the last vefem_assemble. */
+int vefem_last_launch_count(const vefem_ctx *ctx);
+
+/* The CUDA stream the context launches on (cudaStream_t as void*). */
+void *vefem_stream(const vefem_ctx *ctx);
+
+int vefem_destroy(vefem_ctx *ctx);
+
+/* Text of the last error of ctx (or of the last failed vefem_create when ctx is NULL). */
+const char *vefem_last_error(const vefem_ctx *ctx);
+
+/* Host helper: the AIJ pattern preAllocatePetsc freezes (Petsc_mod.F90:629-743)
+ * for a mesh, for hosts without PETSc.  Call once with rowptr/colind NULL to
+ * get n and nnz, then again with arrays of those sizes. */
+int vefem_build_pattern(const vefem_mesh *mesh, int nex, int64_t *n, int64_t *nnz,
+                        int64_t *rowptr, int32_t *colind);
+
+int vefem_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VEFEM_H */

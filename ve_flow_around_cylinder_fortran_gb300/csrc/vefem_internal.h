@@ -1,0 +1,77 @@
+// Internal interface between the C-ABI layer (vefem_capi.cu) and the kernel
+// translation units.  Not part of the public ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace vefem {
+
+// Physics parameters as the kernels read them (one copy per launch, by value).
+struct KParams {
+    int model, form, nex;
+    double ReN, WiN, BvN, VeN, DfN, Wi0, dt, eps;
+};
+
+// Gauss-point tables of the 3x3 rule (Gauss_Quadrangle_mod.F90), [gp][node].
+struct GaussTables {
+    double w[9];
+    double bfn[9][9], dfdc[9][9], dfde[9][9], d2fdc2[9][9], d2fde2[9][9], d2fdce[9][9];
+    // outlet-edge tables: [edge 0..3][gp 0..2][node]
+    double ew[3];
+    double ebfn[4][3][9], edfdc[4][3][9], edfde[4][3][9], ed2c[4][3][9], ed2e[4][3][9],
+        ed2ce[4][3][9];
+};
+
+void gauss_tables_host(GaussTables *t);
+
+// Element-kernel arguments (device pointers).
+struct ElemArgs {
+    int nel, nnodes;
+    const int32_t *conn;   // [9][nel], 0-based
+    const double *xy;      // [2][nnodes]
+    const double *TL;      // [6][nnodes]
+    const double *EU;      // [nex] (device)
+    double *rs;            // residual scratch [(e*9 + jnod)*6 + jeq]
+    double *es;            // Jacobian scratch [((e*81 + jnod*9 + inod)*36 + jeq*6 + ieq]
+    double *as;            // arclength-column scratch [(e*9 + jnod)*6 + jeq]
+};
+
+cudaError_t upload_tables(const GaussTables &t, cudaStream_t s);
+cudaError_t launch_residual64(const ElemArgs &a, const KParams &p, cudaStream_t s);
+cudaError_t launch_fd64(const ElemArgs &a, const KParams &p, cudaStream_t s);
+
+// Outlet open-BC edges: residual and FD Jacobian of each listed edge into edge scratch.
+struct EdgeArgs {
+    int nedge, nel, nnodes;
+    const int32_t *edge_elem;  // [nedge]
+    const int32_t *edge_id;    // [nedge] 1..4
+    const int32_t *conn;
+    const double *xy, *TL, *EU;
+    double *rs;                // [(k*9 + jnod)*6 + jeq]
+    double *es;                // [((k*81 + jnod*9 + inod)*36 + jeq*6 + ieq]
+    double *as;                // [(k*9 + jnod)*6 + jeq]
+};
+cudaError_t launch_edge64(const EdgeArgs &a, const KParams &p, int want_jac, cudaStream_t s);
+
+// Deterministic element-ordered scatter (pull form).
+struct GatherArgs {
+    int nnodes;
+    int nblocks;
+    int nex;
+    const int64_t *rowptr;     // [N+1]
+    const int32_t *nptr;       // [nnodes+1] node -> residual contributors
+    const int32_t *ncon;       // contributor = e*9 + jnod, element order
+    const int32_t *brow;       // [nblocks] row node of each node-pair block
+    const int32_t *boff;       // [nblocks] column offset of the block inside its rows
+    const int32_t *bptr;       // [nblocks+1]
+    const int32_t *bcon;       // contributor = e*81 + jnod*9 + inod, element order
+};
+cudaError_t launch_gather_residual(const GatherArgs &g, const double *rs, double *b,
+                                   cudaStream_t s);
+cudaError_t launch_gather_jacobian(const GatherArgs &g, const double *es, double *vals,
+                                   cudaStream_t s);
+cudaError_t launch_gather_arclength(const GatherArgs &g, const double *as, double *vals,
+                                    cudaStream_t s);
+
+}  // namespace vefem

@@ -1,0 +1,208 @@
+"""Python binding of the C ABI (include/vefem.h) through ctypes.
+
+The class ``BulkAssembler`` mirrors the reference's call
+``setEquationsBulk(Problem, FE, Mesh, Boundary, GaussInt, Sol, basis_p,
+Flag_NR, Elem, LS)`` (Equations_mod.F90:21-55): ``set_equations_bulk(TL, EU,
+flag_nr, b, vals)`` with ``flag_nr`` 'NRP' (residual and Jacobian) or 'MNR'
+(residual only), adding into ``b`` and the AIJ ``vals`` like ADD_VALUES.
+
+The library is loaded from this package's ``_build`` directory; there is no
+CPU fallback: without the built library (or without a GPU) calls fail loudly.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_build", "libvefem.so")
+
+VEFEM_RESIDUAL = 0x1
+VEFEM_JAC_FD64 = 0x2
+VEFEM_ZERO_FIRST = 0x100
+VEFEM_OUTLET_EDGES = 0x200
+VEFEM_TIMING = 0x1000
+
+EXPORTED = ["vefem_abi_version", "vefem_create", "vefem_set_params", "vefem_assemble",
+            "vefem_last_timing", "vefem_last_launch_count", "vefem_stream", "vefem_destroy",
+            "vefem_last_error", "vefem_build_pattern"]
+
+
+class VefemError(RuntimeError):
+    pass
+
+
+class c_params(ctypes.Structure):
+    _fields_ = [("model", ctypes.c_int32), ("form", ctypes.c_int32), ("nex", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("ReN", ctypes.c_double), ("WiN", ctypes.c_double),
+                ("BvN", ctypes.c_double), ("VeN", ctypes.c_double), ("DfN", ctypes.c_double),
+                ("Wi0", ctypes.c_double), ("dt", ctypes.c_double), ("fd_eps", ctypes.c_double)]
+
+
+class c_mesh(ctypes.Structure):
+    _fields_ = [("nnodes", ctypes.c_int32), ("nel", ctypes.c_int32), ("conn", ctypes.c_void_p),
+                ("xyz", ctypes.c_void_p), ("n_outlet_edges", ctypes.c_int32),
+                ("outlet_edge_elem", ctypes.c_void_p), ("outlet_edge_id", ctypes.c_void_p)]
+
+
+class c_csr(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64), ("rowptr", ctypes.c_void_p), ("colind", ctypes.c_void_p)]
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libvefem.so (built by ``build.py``); raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise VefemError(f"{path} is missing: run ve_flow_around_cylinder_fortran_gb300/build.py")
+    L = ctypes.CDLL(path)
+    P = ctypes.c_void_p
+    L.vefem_abi_version.restype = ctypes.c_int
+    L.vefem_create.argtypes = [P, P, P, ctypes.POINTER(P)]
+    L.vefem_set_params.argtypes = [P, P]
+    L.vefem_assemble.argtypes = [P, P, P, ctypes.c_int, P, P, ctypes.c_int]
+    L.vefem_last_timing.argtypes = [P, P, ctypes.c_int]
+    L.vefem_last_launch_count.argtypes = [P]
+    L.vefem_stream.argtypes = [P]
+    L.vefem_stream.restype = P
+    L.vefem_destroy.argtypes = [P]
+    L.vefem_last_error.argtypes = [P]
+    L.vefem_last_error.restype = ctypes.c_char_p
+    L.vefem_build_pattern.argtypes = [P, ctypes.c_int, P, P, P, P]
+    _lib = L
+    return L
+
+
+def _ptr(a) -> int | None:
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):           # torch tensor on the device
+        return a.data_ptr()
+    return int(a)
+
+
+def make_params(phys) -> c_params:
+    from .state import FORMS, MODELS
+    return c_params(MODELS[phys.model], FORMS[phys.form], phys.nex, 0, phys.ReN, phys.WiN,
+                    phys.BvN, phys.VeN, phys.DfN, phys.Wi0, phys.dt, phys.eps)
+
+
+def build_pattern(conn: np.ndarray, nnodes: int, nex: int):
+    """AIJ pattern of preAllocatePetsc through the library's host helper."""
+    L = load()
+    conn = np.ascontiguousarray(conn, dtype=np.int32)
+    m = c_mesh(nnodes, conn.shape[1], conn.ctypes.data, None, 0, None, None)
+    n = ctypes.c_int64()
+    nnz = ctypes.c_int64()
+    rc = L.vefem_build_pattern(ctypes.byref(m), nex, ctypes.byref(n), ctypes.byref(nnz), None, None)
+    if rc:
+        raise VefemError(L.vefem_last_error(None).decode())
+    rowptr = np.zeros(n.value + 1, dtype=np.int64)
+    colind = np.zeros(nnz.value, dtype=np.int32)
+    rc = L.vefem_build_pattern(ctypes.byref(m), nex, ctypes.byref(n), ctypes.byref(nnz),
+                               rowptr.ctypes.data, colind.ctypes.data)
+    if rc:
+        raise VefemError(L.vefem_last_error(None).decode())
+    return rowptr, colind
+
+
+class BulkAssembler:
+    """One mesh, one frozen AIJ pattern, one physics parameter set."""
+
+    def __init__(self, mesh, phys, rowptr: np.ndarray, colind: np.ndarray,
+                 outlet_edges: bool = False):
+        L = load()
+        self._L = L
+        self.phys = phys
+        self._conn = np.ascontiguousarray(mesh.conn, dtype=np.int32)
+        self._xyz = np.ascontiguousarray(mesh.xyz, dtype=np.float64)
+        self.rowptr = np.ascontiguousarray(rowptr, dtype=np.int64)
+        self.colind = np.ascontiguousarray(colind, dtype=np.int32)
+        self.nnodes = int(mesh.nnodes)
+        self.nel = int(mesh.nel)
+        self.N = int(self.rowptr.shape[0] - 1)
+        self.nnz = int(self.colind.shape[0])
+        if outlet_edges and len(mesh.outlet_edges):
+            self._ee = np.ascontiguousarray(mesh.outlet_edges[:, 0], dtype=np.int32)
+            self._ei = np.ascontiguousarray(mesh.outlet_edges[:, 1], dtype=np.int32)
+            ne = len(self._ee)
+        else:
+            self._ee = self._ei = None
+            ne = 0
+        cm = c_mesh(self.nnodes, self.nel, self._conn.ctypes.data, self._xyz.ctypes.data, ne,
+                    _ptr(self._ee), _ptr(self._ei))
+        cc = c_csr(self.N, self.rowptr.ctypes.data, self.colind.ctypes.data)
+        self._params = make_params(phys)
+        h = ctypes.c_void_p()
+        rc = L.vefem_create(ctypes.byref(cm), ctypes.byref(cc), ctypes.byref(self._params),
+                            ctypes.byref(h))
+        if rc:
+            raise VefemError(f"vefem_create failed ({rc}): {L.vefem_last_error(None).decode()}")
+        self._h = h
+
+    def _check(self, rc):
+        if rc:
+            raise VefemError(f"vefem error {rc}: {self._L.vefem_last_error(self._h).decode()}")
+
+    def set_params(self, phys):
+        self.phys = phys
+        self._params = make_params(phys)
+        self._check(self._L.vefem_set_params(self._h, ctypes.byref(self._params)))
+
+    def assemble(self, TL, EU, flags: int, b=None, vals=None, on_device: bool = False):
+        """Raw entry point: arrays are numpy (host) or torch CUDA tensors (device)."""
+        self._check(self._L.vefem_assemble(self._h, _ptr(TL), _ptr(EU), int(flags), _ptr(b),
+                                           _ptr(vals), 1 if on_device else 0))
+
+    def set_equations_bulk(self, TL, EU, flag_nr: str = "NRP", b=None, vals=None,
+                           zero_first: bool = False, outlet_edges: bool = False):
+        """setEquationsBulk on host arrays; returns (b, vals)."""
+        if flag_nr not in ("NRP", "MNR"):
+            raise ValueError("flag_nr must be 'NRP' or 'MNR'")
+        TL = np.ascontiguousarray(TL, dtype=np.float64)
+        EU = np.ascontiguousarray(EU if EU is not None and len(EU) else np.zeros(1), dtype=np.float64)
+        if b is None:
+            b = np.zeros(self.N)
+        flags = VEFEM_RESIDUAL
+        if flag_nr == "NRP":
+            flags |= VEFEM_JAC_FD64
+            if vals is None:
+                vals = np.zeros(self.nnz)
+        else:
+            vals = None
+        if zero_first:
+            flags |= VEFEM_ZERO_FIRST
+        if outlet_edges:
+            flags |= VEFEM_OUTLET_EDGES
+        self.assemble(TL, EU, flags, b, vals, on_device=False)
+        return b, vals
+
+    def last_timing(self):
+        t = (ctypes.c_float * 5)()
+        self._check(self._L.vefem_last_timing(self._h, t, 5))
+        return list(t)
+
+    def last_launch_count(self) -> int:
+        return int(self._L.vefem_last_launch_count(self._h))
+
+    def stream(self) -> int:
+        return int(self._L.vefem_stream(self._h) or 0)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.vefem_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
