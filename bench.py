@@ -1,0 +1,374 @@
+#!/usr/bin/env python
+"""Benchmark of the element assembly on GB300.
+
+Workload (one "step"): one Newton 'NRP' bulk assembly -- setEquationsBulk with
+the FP64 residual and the FP64 forward-difference Jacobian (56 residual
+evaluations per element, the reference algorithm, bit-exact) -- on the
+cylinder-in-channel mesh with 40,000 Q2 quads, Giesekus alpha = 0.1,
+beta = 0.59, Wi = 0.5, square-root conformation (SQRT) form, arclength
+unknown (Nex = 1).  Synthetic seeded state (no dataset exists for this path).
+
+* value: elements/s with the state resident in HBM (vefem_assemble with
+  device pointers), CUDA events on the library's stream over the timed steps;
+* e2e: the same metric through the C ABI with pinned host buffers: the host
+  TL/EU go in and the residual and all AIJ values come back every step;
+* roofline: the FD kernel is bound by the FP64 pipe; achieved = algorithmic
+  FP64 operations per launch (counted from the kernel source, see
+  vefem_algorithmic_ops) / its event-timed duration, peak = the FP64
+  instruction rate measured live on this GPU by a probe kernel;
+* cpu_baseline: the CPU oracle (a C restatement of the reference algorithm)
+  on all host cores, on a bounded sample of the same workload.
+
+``--impl reference`` times that CPU implementation as the reference arm.
+Multi-GPU: the assembly of one mesh does not shard across GPUs in this
+library (replicas only): under torchrun every rank runs its own instance and
+``value`` is the total over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+from ve_flow_around_cylinder_fortran_gb300 import build as B  # noqa: E402
+from ve_flow_around_cylinder_fortran_gb300 import mesh as M  # noqa: E402
+from ve_flow_around_cylinder_fortran_gb300 import pattern as P  # noqa: E402
+from ve_flow_around_cylinder_fortran_gb300 import state as S  # noqa: E402
+from ve_flow_around_cylinder_fortran_gb300 import vefem as V  # noqa: E402
+
+METRIC = "Continuation steps/s learned+mixed vs plain FP64 GPU at ||R||<1e-10; elem/s"
+UNIT = "elem/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["vefem", "reference"], default="vefem")
+    ap.add_argument("--nel", type=int, default=40000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload(nel: int):
+    mesh = M.build_cylinder_mesh(nel)
+    phys = S.giesekus(alpha=0.1, Wi=0.5, beta=0.59, form="SQRT", nex=1)
+    TL, EU = S.seeded_state(mesh.xyz, phys, seed=0)
+    rowptr, colind = P.build_pattern(mesh.element_nodes(), mesh.nnodes, phys.nex)
+    cfg = {
+        "workload": f"cylinder-in-channel (R=1, y in [-2,2], x in [-15,25]), {mesh.nel} Q2 quads, "
+                    "Giesekus alpha=0.1, beta=0.59, Wi=0.5, SQRT form, Nex=1; one Newton 'NRP' "
+                    "bulk assembly: FP64 residual + FP64 forward-difference Jacobian into AIJ",
+        "nel": mesh.nel, "nnodes": mesh.nnodes, "dofs": int(len(rowptr) - 1),
+        "nnz": int(len(colind)), "seed": 0,
+        "l2": "no flush: every step streams > 1 GB (element scratch + AIJ values), "
+              "well above the 129 MB L2",
+    }
+    return mesh, phys, TL, EU, rowptr, colind, cfg
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,utilization.gpu,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-i", str(self.device), "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 10:
+                continue
+            try:
+                rows.append(dict(sm=float(f[1]), smax=float(f[2]), power=float(f[3]),
+                                 util=float(f[4]), hw=f[6], hwt=f[7], swt=f[8], swp=f[9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return None
+        load = [r for r in rows if r["util"] >= 50] or rows
+        reasons = set()
+        for r in load:
+            for k, name in (("hw", "hw_slowdown"), ("hwt", "hw_thermal_slowdown"),
+                            ("swt", "sw_thermal_slowdown"), ("swp", "sw_power_cap")):
+                if r[k].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(r["sm"] for r in load),
+                "sm_max_mhz": max(r["smax"] for r in load), "samples": len(load),
+                "reasons": sorted(reasons)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return world, rank, local, dist
+
+
+def fp64_peak(device: int):
+    lib = ctypes.CDLL(B.PROBE)
+    lib.vefem_probe_fp64.argtypes = [ctypes.c_int, ctypes.c_void_p]
+    out = np.zeros(3)
+    rc = lib.vefem_probe_fp64(device, out.ctypes.data)
+    if rc:
+        raise RuntimeError(f"FP64 probe failed: {rc}")
+    return {"dfma_inst_per_s": out[0], "dadd_inst_per_s": out[1], "dmul_inst_per_s": out[2]}
+
+
+def algorithmic_ops(phys, flags):
+    L = V.load()
+    L.vefem_algorithmic_ops.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+    out = np.zeros(6)
+    p = V.make_params(phys)
+    if L.vefem_algorithmic_ops(ctypes.byref(p), flags, out.ctypes.data):
+        raise RuntimeError("vefem_algorithmic_ops failed")
+    return out
+
+
+def cpu_oracle_rate(phys, mesh, TL, EU, rowptr, colind, target_s: float, reps: int):
+    """Elements/s of the oracle assembly on all host cores, on the first n
+    elements of the mesh, n sized for about target_s seconds per repetition."""
+    from oracle import oracle as O
+    cores = os.cpu_count() or 1
+    conn = mesh.conn
+    n0 = min(mesh.nel, 512)
+    t = time.perf_counter()
+    O.assemble(phys, np.ascontiguousarray(conn[:, :n0]), mesh.xyz, TL, EU, rowptr, colind,
+               nthreads=cores)
+    rate0 = n0 / (time.perf_counter() - t)
+    n = int(min(mesh.nel, max(n0, rate0 * target_s)))
+    sub = np.ascontiguousarray(conn[:, :n])
+    times = []
+    for _ in range(reps):
+        t = time.perf_counter()
+        O.assemble(phys, sub, mesh.xyz, TL, EU, rowptr, colind, nthreads=cores)
+        times.append(time.perf_counter() - t)
+    return n / statistics.median(times), n, cores, times
+
+
+def traffic_per_element():
+    path = os.path.join(ROOT, "profiles", "k_fd64_dram.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return d.get("dram_bytes_per_element")
+    return None
+
+
+def run_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    mesh, phys, TL, EU, rowptr, colind, cfg = workload(args.nel)
+    from oracle import oracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    # size each step as a bounded sample of the workload (about 3 s of CPU work)
+    _, n, _, _ = cpu_oracle_rate(phys, mesh, TL, EU, rowptr, colind, 3.0, 1)
+    sub = np.ascontiguousarray(mesh.conn[:, :n])
+    for _ in range(args.warmup):
+        O.assemble(phys, sub, mesh.xyz, TL, EU, rowptr, colind, nthreads=cores)
+    times = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        O.assemble(phys, sub, mesh.xyz, TL, EU, rowptr, colind, nthreads=cores)
+        times.append(time.perf_counter() - t)
+    total = sum(times)
+    value = n * args.steps / total
+    sample = f"first {n} of {mesh.nel} elements per step (full residual + FD Jacobian into AIJ)"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": cfg,
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference (Fortran + PETSc + MPI) cannot be built on this machine or the "
+                "GPU box (no Fortran compiler); its algorithm runs as the C oracle port, "
+                "OpenMP over elements, sequential element-ordered AIJ adds",
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_vefem(args):
+    import torch
+    world, rank, local, dist = dist_setup()
+    dev = local
+    torch.cuda.set_device(dev)
+    B.build()
+    mesh, phys, TL, EU, rowptr, colind, cfg = workload(args.nel)
+    asm = V.BulkAssembler(mesh, phys, rowptr, colind, device=dev)
+    nel = mesh.nel
+    d = torch.device(f"cuda:{dev}")
+    tTL = torch.from_numpy(TL).to(d)
+    tEU = torch.from_numpy(EU).to(d)
+    tb = torch.zeros(asm.N, dtype=torch.float64, device=d)
+    tv = torch.zeros(asm.nnz, dtype=torch.float64, device=d)
+    flags = V.VEFEM_RESIDUAL | V.VEFEM_JAC_FD64 | V.VEFEM_ZERO_FIRST | V.VEFEM_TIMING
+    torch.cuda.synchronize()
+    stream = torch.cuda.ExternalStream(asm.stream(), device=d)
+
+    # ---- device-resident timed region
+    for _ in range(args.warmup):
+        asm.assemble(tTL, tEU, flags, tb, tv, on_device=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(dev)
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    k_times = []
+    launches = 0
+    for _ in range(args.steps):
+        asm.assemble(tTL, tEU, flags, tb, tv, on_device=True)
+        t = asm.last_timing()
+        k_times.append(t[0])
+        launches += asm.last_launch_count()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    if dist:
+        tm = torch.tensor([ms], device=d)
+        dist.all_reduce(tm, op=dist.ReduceOp.MAX)
+        ms = float(tm.item())
+    value = world * nel * args.steps / (ms * 1e-3)
+
+    # ---- residual-only ('MNR') on the same state
+    rflags = V.VEFEM_RESIDUAL | V.VEFEM_ZERO_FIRST | V.VEFEM_TIMING
+    for _ in range(args.warmup):
+        asm.assemble(tTL, tEU, rflags, tb, None, on_device=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    r_k = []
+    for _ in range(args.steps):
+        asm.assemble(tTL, tEU, rflags, tb, None, on_device=True)
+        r_k.append(asm.last_timing()[0])
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    r_ms = ev0.elapsed_time(ev1)
+
+    # ---- end to end through the C ABI with pinned host buffers
+    hTL = torch.from_numpy(TL).pin_memory().numpy()
+    hEU = torch.from_numpy(EU).pin_memory().numpy()
+    hb = torch.zeros(asm.N, dtype=torch.float64).pin_memory().numpy()
+    hv = torch.zeros(asm.nnz, dtype=torch.float64).pin_memory().numpy()
+    eflags = V.VEFEM_RESIDUAL | V.VEFEM_JAC_FD64 | V.VEFEM_ZERO_FIRST
+    for _ in range(args.warmup):
+        asm.assemble(hTL, hEU, eflags, hb, hv, on_device=False)
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        asm.assemble(hTL, hEU, eflags, hb, hv, on_device=False)
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        te = torch.tensor([e2e_s], device=d)
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+        e2e_s = float(te.item())
+    e2e = {"value": world * nel * args.steps / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": int(hTL.nbytes + hEU.nbytes),
+           "d2h_bytes_per_step": int(hb.nbytes + hv.nbytes)}
+
+    if rank != 0:
+        asm.close()
+        dist.destroy_process_group()
+        return 0
+
+    # ---- roofline of the dominant kernel (FD Jacobian kernel, FP64 pipe bound)
+    peaks = fp64_peak(dev)
+    ops = algorithmic_ops(phys, flags)
+    k_avg_ms = statistics.mean(k_times)
+    achieved = ops[0] * nel / (k_avg_ms * 1e-3)
+    peak = peaks["dfma_inst_per_s"]
+    tpe = traffic_per_element()
+    roof = {"kernel": "k_fd64<SQRT>", "bound": "fp64", "achieved": achieved / 1e12,
+            "peak": peak / 1e12, "unit": "TOP/s", "frac": achieved / peak,
+            "traffic": (tpe * nel if tpe else None),
+            "ops_per_element": ops[0], "ops_split": {"add": ops[1], "mul": ops[2], "div": ops[3],
+                                                     "sqrt": ops[4], "exp": ops[5]},
+            "kernel_ms_avg": k_avg_ms, "kernel_share_of_step": k_avg_ms / (ms / args.steps),
+            "peak_source": "measured live: FP64 DFMA instruction rate of a probe kernel "
+                           "(one instruction = one operation; this path cannot use FMA)",
+            "dadd_peak": peaks["dadd_inst_per_s"] / 1e12, "dmul_peak": peaks["dmul_inst_per_s"] / 1e12}
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        rate, n, cores, times = cpu_oracle_rate(phys, mesh, TL, EU, rowptr, colind, 6.0, 3)
+        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"first {n} of {nel} elements, residual + FD Jacobian into AIJ, "
+                         f"median of 3 ({', '.join(f'{x:.2f}' for x in times)} s)"}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": cfg, "e2e": e2e, "gpu_launches": launches, "roofline": roof,
+        "cpu_baseline": cpu, "clocks": clk,
+        "residual_only": {"value": nel * args.steps / (r_ms * 1e-3), "unit": UNIT,
+                          "kernel_ms_avg": statistics.mean(r_k)},
+    }
+    print(json.dumps(line))
+    asm.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_vefem(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

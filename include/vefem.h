@@ -82,7 +82,7 @@ typedef struct vefem_params {
     int32_t model;
     int32_t form;
     int32_t nex;                 /* 0 or 1 */
-    int32_t reserved;
+    int32_t device;              /* CUDA device ordinal the context runs on */
     double ReN, WiN, BvN, VeN, DfN, Wi0, dt, fd_eps;
 } vefem_params;
 
@@ -149,6 +149,14 @@ const char *vefem_last_error(const vefem_ctx *ctx);
  * get n and nnz, then again with arrays of those sizes. */
 int vefem_build_pattern(const vefem_mesh *mesh, int nex, int64_t *n, int64_t *nnz,
                         int64_t *rowptr, int32_t *colind);
+
+/* Algorithmic FP64 operation count per element of the element kernel that
+ * vefem_assemble runs for these flags (VEFEM_JAC_FD64 set: residual + FD
+ * Jacobian, 56 residual evaluations; else the residual alone), obtained by
+ * running the kernels' own physics source with an op-counting scalar.
+ * out[0] = total (+, -, *, /, sqrt, exp count one each), out[1..5] = the
+ * add/sub, mul, div, sqrt and exp parts.  Used for roofline reporting. */
+int vefem_algorithmic_ops(const vefem_params *params, int flags, double *out);
 
 int vefem_abi_version(void);
 

@@ -27,6 +27,7 @@
 using namespace vefem;
 
 struct vefem_ctx {
+    int device = 0;
     int nnodes = 0, nel = 0, nex = 0;
     int64_t N = 0, nnz = 0;
     int nblocks = 0;
@@ -225,6 +226,7 @@ static int check_params(const vefem_params *p, std::string &why)
     if (p->form != VEFEM_FORM_T && p->form != VEFEM_FORM_SQRT) { why = "form must be T or SQRT"; return 0; }
     if (p->nex < 0 || p->nex > 1) { why = "nex must be 0 or 1"; return 0; }
     if (!(p->fd_eps > 0.0)) { why = "fd_eps must be positive"; return 0; }
+    if (p->device < 0) { why = "device must be >= 0"; return 0; }
     return 1;
 }
 
@@ -273,6 +275,7 @@ extern "C" int vefem_create(const vefem_mesh *mesh, const vefem_csr *pat,
 
     ctx = new (std::nothrow) vefem_ctx();
     if (!ctx) return fail(nullptr, VEFEM_ERR_NOMEM, "host allocation");
+    ctx->device = params->device;
     ctx->nnodes = nn;
     ctx->nel = nel;
     ctx->nex = nex;
@@ -403,7 +406,8 @@ extern "C" int vefem_create(const vefem_mesh *mesh, const vefem_csr *pat,
     ctx->nblocks = nblocks;
     ctx->nedge = nedge;
 
-    cudaError_t ce = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    cudaError_t ce = cudaSetDevice(ctx->device);
+    if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (ce != cudaSuccess) {
         std::string m = std::string("cudaStreamCreate: ") + cudaGetErrorString(ce);
         delete ctx;
@@ -453,6 +457,7 @@ extern "C" int vefem_set_params(vefem_ctx *ctx, const vefem_params *p)
     std::string why;
     if (!check_params(p, why)) return fail(ctx, VEFEM_ERR_ARG, why);
     if (p->nex != ctx->nex) return fail(ctx, VEFEM_ERR_ARG, "nex is fixed by the pattern");
+    if (p->device != ctx->device) return fail(ctx, VEFEM_ERR_ARG, "device is fixed at create");
     ctx->prm = to_kparams(p);
     return VEFEM_OK;
 }
@@ -479,6 +484,7 @@ extern "C" int vefem_assemble(vefem_ctx *ctx, const double *TL, const double *EU
     if (ctx->nex > 0 && !EU) return fail(ctx, VEFEM_ERR_ARG, "EU is NULL with nex = 1");
     if (want_res && !b) return fail(ctx, VEFEM_ERR_ARG, "b is NULL");
     if (want_jac && !vals) return fail(ctx, VEFEM_ERR_ARG, "vals is NULL");
+    CK(cudaSetDevice(ctx->device));
     cudaStream_t s = ctx->stream;
     const size_t nel = ctx->nel, nn = ctx->nnodes;
     ctx->launches = 0;
@@ -630,6 +636,7 @@ extern "C" void *vefem_stream(const vefem_ctx *ctx) { return ctx ? (void *)ctx->
 extern "C" int vefem_destroy(vefem_ctx *ctx)
 {
     if (!ctx) return VEFEM_OK;
+    cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     void *ptrs[] = {ctx->d_conn, ctx->d_xy, ctx->d_rowptr, ctx->d_nptr, ctx->d_ncon, ctx->d_brow,
                     ctx->d_boff, ctx->d_bptr, ctx->d_bcon, ctx->d_edge_elem, ctx->d_edge_id,

@@ -36,7 +36,7 @@ class VefemError(RuntimeError):
 
 class c_params(ctypes.Structure):
     _fields_ = [("model", ctypes.c_int32), ("form", ctypes.c_int32), ("nex", ctypes.c_int32),
-                ("reserved", ctypes.c_int32), ("ReN", ctypes.c_double), ("WiN", ctypes.c_double),
+                ("device", ctypes.c_int32), ("ReN", ctypes.c_double), ("WiN", ctypes.c_double),
                 ("BvN", ctypes.c_double), ("VeN", ctypes.c_double), ("DfN", ctypes.c_double),
                 ("Wi0", ctypes.c_double), ("dt", ctypes.c_double), ("fd_eps", ctypes.c_double)]
 
@@ -89,9 +89,9 @@ def _ptr(a) -> int | None:
     return int(a)
 
 
-def make_params(phys) -> c_params:
+def make_params(phys, device: int = 0) -> c_params:
     from .state import FORMS, MODELS
-    return c_params(MODELS[phys.model], FORMS[phys.form], phys.nex, 0, phys.ReN, phys.WiN,
+    return c_params(MODELS[phys.model], FORMS[phys.form], phys.nex, device, phys.ReN, phys.WiN,
                     phys.BvN, phys.VeN, phys.DfN, phys.Wi0, phys.dt, phys.eps)
 
 
@@ -118,7 +118,7 @@ class BulkAssembler:
     """One mesh, one frozen AIJ pattern, one physics parameter set."""
 
     def __init__(self, mesh, phys, rowptr: np.ndarray, colind: np.ndarray,
-                 outlet_edges: bool = False):
+                 outlet_edges: bool = False, device: int = 0):
         L = load()
         self._L = L
         self.phys = phys
@@ -140,7 +140,8 @@ class BulkAssembler:
         cm = c_mesh(self.nnodes, self.nel, self._conn.ctypes.data, self._xyz.ctypes.data, ne,
                     _ptr(self._ee), _ptr(self._ei))
         cc = c_csr(self.N, self.rowptr.ctypes.data, self.colind.ctypes.data)
-        self._params = make_params(phys)
+        self.device = device
+        self._params = make_params(phys, device)
         h = ctypes.c_void_p()
         rc = L.vefem_create(ctypes.byref(cm), ctypes.byref(cc), ctypes.byref(self._params),
                             ctypes.byref(h))
@@ -154,7 +155,7 @@ class BulkAssembler:
 
     def set_params(self, phys):
         self.phys = phys
-        self._params = make_params(phys)
+        self._params = make_params(phys, self.device)
         self._check(self._L.vefem_set_params(self._h, ctypes.byref(self._params)))
 
     def assemble(self, TL, EU, flags: int, b=None, vals=None, on_device: bool = False):
