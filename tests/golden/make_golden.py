@@ -1,6 +1,8 @@
 """Generates tests/golden/golden.json: SHA-256 digests (and a few sampled
 values) of the oracle's element residuals, FD Jacobians and arclength columns
-for small seeded cases.  The digests pin the exact bits: the oracle must keep
+for small seeded cases.  The inputs come from ``state.portable_state``
+(uniform draws and elementwise IEEE arithmetic only) so they are the same
+bits on every machine.  The digests pin the exact bits: the oracle must keep
 producing them (CPU test), and the CUDA library must produce the same bits
 (GPU test).  Models that call exp() are left out (libm's last bit is not
 portable across machines).
@@ -48,7 +50,7 @@ def digest(a):
 def run_case(c):
     mesh = case_mesh(c)
     phys = case_phys(c)
-    TL, EU = S.seeded_state(mesh.xyz, phys, c["seed"])
+    TL, EU = S.portable_state(mesh.xyz, phys, c["seed"])
     res, jac, ac = O.element_outputs(phys, mesh.conn, mesh.xyz, TL, EU)
     return mesh, phys, TL, EU, res, jac, ac
 

@@ -37,7 +37,7 @@ def test_library_reproduces_golden(entry):
     mesh = G.case_mesh(c)
     phys = G.case_phys(c)
     from ve_flow_around_cylinder_fortran_gb300 import state as S
-    TL, EU = S.seeded_state(mesh.xyz, phys, c["seed"])
+    TL, EU = S.portable_state(mesh.xyz, phys, c["seed"])
     # element-duplicated copy (like the reference's TL_Rank): node 9*e + i
     en = mesh.element_nodes()
     nel = mesh.nel

@@ -12,7 +12,8 @@ the workloads are quoted on:
 * SQRT form unknowns: S = c^(1/2) (symmetric square root)
 
 Draw order from ``numpy.random.default_rng(seed)``: u-noise (Nnodes), v
-(Nnodes), p (Nnodes), A (Nnodes x 2 x 2).
+(Nnodes), p (Nnodes), A (Nnodes x 2 x 2).  ``portable_state`` draws uniform
+numbers instead (exact across machines) for fixtures whose bits are recorded.
 
 Field order and layout follow the reference: TL(Nnodes, Neq) column-major,
 i.e. a C array [6, Nnodes] with rows Ux, Uy, P, Txx, Txy, Tyy
@@ -73,13 +74,19 @@ def giesekus(alpha: float = 0.1, Wi: float = 0.5, beta: float = 0.59, form: str 
 
 
 def conformation_to_unknowns(c: np.ndarray, phys: Physics) -> np.ndarray:
-    """c [n, 2, 2] SPD -> (Txx, Txy, Tyy) or (Sxx, Sxy, Syy) per node, [3, n]."""
+    """c [n, 2, 2] SPD -> (Txx, Txy, Tyy) or (Sxx, Sxy, Syy) per node, [3, n].
+
+    The square root of a 2x2 SPD matrix is taken in closed form,
+    S = (c + sqrt(det c) I) / sqrt(tr c + 2 sqrt(det c)), with elementwise
+    IEEE operations only, so the same seed gives the same bits on every
+    machine (a LAPACK eigensolver would not)."""
+    a, b, d = c[:, 0, 0], c[:, 0, 1], c[:, 1, 1]
     if phys.form == "SQRT":
-        w, v = np.linalg.eigh(c)
-        s = np.einsum("nij,nj,nkj->nik", v, np.sqrt(w), v)
-        return np.stack([s[:, 0, 0], s[:, 0, 1], s[:, 1, 1]])
-    t = (1.0 - phys.BvN) / phys.WiN * (c - np.eye(2)[None])
-    return np.stack([t[:, 0, 0], t[:, 0, 1], t[:, 1, 1]])
+        sd = np.sqrt(a * d - b * b)
+        t = np.sqrt(a + d + 2.0 * sd)
+        return np.stack([(a + sd) / t, b / t, (d + sd) / t])
+    k = (1.0 - phys.BvN) / phys.WiN
+    return np.stack([k * (a - 1.0), k * b, k * (d - 1.0)])
 
 
 def seeded_state(xyz: np.ndarray, phys: Physics, seed: int = 0, R: float = 1.0, H: float = 2.0,
@@ -94,9 +101,37 @@ def seeded_state(xyz: np.ndarray, phys: Physics, seed: int = 0, R: float = 1.0, 
     v = rng.normal(0.0, 0.01, n)
     p = rng.normal(0.0, 0.01, n)
     A = rng.normal(0.0, 0.1, (n, 2, 2))
-    c = np.eye(2)[None] + 0.1 * np.einsum("nij,nkj->nik", A, A)
+    c = np.empty((n, 2, 2))
+    c[:, 0, 0] = 1.0 + 0.1 * (A[:, 0, 0] * A[:, 0, 0] + A[:, 0, 1] * A[:, 0, 1])
+    c[:, 0, 1] = 0.1 * (A[:, 0, 0] * A[:, 1, 0] + A[:, 0, 1] * A[:, 1, 1])
+    c[:, 1, 0] = c[:, 0, 1]
+    c[:, 1, 1] = 1.0 + 0.1 * (A[:, 1, 0] * A[:, 1, 0] + A[:, 1, 1] * A[:, 1, 1])
     TL = np.empty((6, n))
     TL[0], TL[1], TL[2] = u, v, p
+    TL[3:] = conformation_to_unknowns(c, phys)
+    EU = np.full(phys.nex, arn, dtype=np.float64)
+    if phys.nex:
+        phys.Wi0 = phys.WiN / arn
+    return np.ascontiguousarray(TL), EU
+
+
+def portable_state(xyz: np.ndarray, phys: Physics, seed: int = 0, arn: float = 1.0):
+    """A state built only from uniform draws (53-bit integers scaled by 2^-53)
+    and elementwise IEEE operations, so its bits are the same on every
+    machine: u in [1, 1.5), v and p in [-0.05, 0.05), conformation
+    c = I + 0.1 B with B symmetric, entries in [-0.1, 0.1) (diagonal in [0, 0.1))."""
+    rng = np.random.default_rng(seed)
+    n = xyz.shape[1]
+    r = rng.random((7, n))
+    TL = np.empty((6, n))
+    TL[0] = 1.0 + 0.5 * r[0]
+    TL[1] = 0.1 * (r[1] - 0.5)
+    TL[2] = 0.1 * (r[2] - 0.5)
+    c = np.empty((n, 2, 2))
+    c[:, 0, 0] = 1.0 + 0.1 * (0.1 * r[3])
+    c[:, 0, 1] = 0.1 * (0.2 * (r[4] - 0.5))
+    c[:, 1, 0] = c[:, 0, 1]
+    c[:, 1, 1] = 1.0 + 0.1 * (0.1 * r[5])
     TL[3:] = conformation_to_unknowns(c, phys)
     EU = np.full(phys.nex, arn, dtype=np.float64)
     if phys.nex:
