@@ -158,6 +158,24 @@ int vefem_build_pattern(const vefem_mesh *mesh, int nex, int64_t *n, int64_t *nn
  * add/sub, mul, div, sqrt and exp parts.  Used for roofline reporting. */
 int vefem_algorithmic_ops(const vefem_params *params, int flags, double *out);
 
+/* Residual-only bulk assembly ('MNR') that allocates no device memory.  No
+ * counterpart in the reference: it exists for callers that cannot call
+ * cudaMalloc when they assemble (device memory owned by another allocator or
+ * pool, allocation-free sections, no long-lived library context).
+ * All pointers are device pointers: conn [9*nel] (Connectivity(Nel,9),
+ * 1-based), xyz [3*nnodes], TL [6*nnodes], EU [nex], b [nnodes*6 + nex];
+ * the residual is ADDED into b (rows of the arclength unknown untouched),
+ * bit-identical to vefem_assemble(VEFEM_RESIDUAL).  stream: a cudaStream_t
+ * (NULL = default stream); the call returns after the stream has finished.
+ * Scratch is one static device array of about 17.7 MB that every GPU loading
+ * the library holds until exit; meshes above 32768 elements or 294912 nodes
+ * are rejected with VEFEM_ERR_ARG.  The first call on a device looks up that
+ * array's address and uploads the Gauss tables: make it before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race. */
+int vefem_assemble_residual_noalloc(const vefem_params *params, int nnodes, int nel,
+                                    const int32_t *conn, const double *xyz, const double *TL,
+                                    const double *EU, double *b, void *stream);
+
 int vefem_abi_version(void);
 
 #ifdef __cplusplus

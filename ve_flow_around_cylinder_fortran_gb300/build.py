@@ -20,7 +20,8 @@ LIB = os.path.join(OUT, "libvefem.so")
 PROBE = os.path.join(OUT, "libvefem_probe.so")
 INCLUDE = os.path.join(ROOT, "include")
 
-SOURCES = ["vefem_fd64.cu", "vefem_gather.cu", "vefem_capi.cu", "vefem_opcount.cpp"]
+SOURCES = ["vefem_fd64.cu", "vefem_gather.cu", "vefem_capi.cu", "vefem_opcount.cpp",
+           "vefem_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

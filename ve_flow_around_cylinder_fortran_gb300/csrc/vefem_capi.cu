@@ -54,6 +54,8 @@ struct vefem_ctx {
 
 static std::string g_create_error;
 
+void vefem::set_global_error(const std::string &msg) { g_create_error = msg; }
+
 namespace vefem {
 
 // Gauss_Quadrangle_mod.F90: setQuadraticQuadrangle :405-478 (same expression

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 namespace vefem {
 
 // Physics parameters as the kernels read them (one copy per launch, by value).
@@ -73,5 +75,8 @@ cudaError_t launch_gather_jacobian(const GatherArgs &g, const double *es, double
                                    cudaStream_t s);
 cudaError_t launch_gather_arclength(const GatherArgs &g, const double *as, double *vals,
                                     cudaStream_t s);
+
+// Message returned by vefem_last_error(NULL) for entry points without a context.
+void set_global_error(const std::string &msg);
 
 }  // namespace vefem
