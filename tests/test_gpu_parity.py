@@ -205,3 +205,16 @@ def test_cylinder_40000_giesekus_sqrt_bitwise():
     _, _, _, _, b, vals, bo, vo = _case(mesh, phys, seed=0)
     _compare("GIESEKUS", b, bo, "residual")
     _compare("GIESEKUS", vals, vo, "jacobian")
+
+
+@pytest.mark.parametrize("form", ["T", "SQRT"])
+@pytest.mark.parametrize("DfN", [0.0, 1.0e-3])
+def test_reynolds_nonzero(form, DfN):
+    """Re > 0 and DfN > 0 take the kernel variants that keep the convection,
+    LSME-momentum and diffusion terms (the Re = 0 / DfN = 0 variants drop them)."""
+    mesh = M.build_cylinder_mesh(2000)
+    phys = S.Physics(model="GIESEKUS", form=form, ReN=0.7, WiN=0.5, Wi0=0.5, BvN=0.59, VeN=0.1,
+                     nex=1, DfN=DfN)
+    _, _, _, _, b, vals, bo, vo = _case(mesh, phys, seed=8)
+    _compare("GIESEKUS", b, bo, "residual")
+    _compare("GIESEKUS", vals, vo, "jacobian")

@@ -16,8 +16,12 @@
 //    base residual, k = 1..54 the column (inod, ieq) = divmod(k-1, 6), k = 55
 //    the arclength column.  The element state each evaluation sees (with the
 //    (x+eps)-eps restore residue of the earlier columns) is staged once per
-//    element in shared memory; state-independent geometry (basis2D) is
-//    computed once per element and Gauss point.
+//    element in shared memory; state-independent geometry (basis2D) and the
+//    interpolants of the unperturbed state are computed once per element and
+//    Gauss point, so an evaluation recomputes only its perturbed field's
+//    sums (the same sums in the same order; elements with a restore residue
+//    take the full path).  Terms that are exact zeros for Re = 0 or DfN = 0
+//    are left out by template specialisation.
 //  * k_res64: residual only ('MNR'): one thread per (element, Gauss point),
 //    followed by an in-order sum over the Gauss points in shared memory.
 #include <cuda_runtime.h>
@@ -71,6 +75,11 @@ cudaError_t upload_tables(const GaussTables &t, cudaStream_t s)
 // ---------------------------------------------------------------------------
 // FD kernel
 
+struct SmemView {
+    const double *p;
+    __device__ __forceinline__ double operator()(int pos) const { return p[pos]; }
+};
+
 constexpr int FD_EPB = 4;        // elements per CTA
 constexpr int FD_NEV = 56;       // evaluations per element (base + 54 + arclength)
 constexpr int FD_THREADS = FD_EPB * FD_NEV;
@@ -79,7 +88,9 @@ struct FdSmem {
     double tl[FD_EPB][3][54];    // 0: original, 1: restored (x+eps)-eps, 2: perturbed x+eps
     double dFx[FD_EPB][9][9], dFy[FD_EPB][9][9], d2x[FD_EPB][9][9], d2y[FD_EPB][9][9];
     double H2[FD_EPB][9], WET[FD_EPB][9];
+    Interp<double> base[FD_EPB][9];   // interpolants of the original state per Gauss point
     double res0[FD_EPB][54];
+    int residue[FD_EPB];         // 1 if some (x+eps)-eps differs from x in the element
 };
 
 // the state evaluation k sees: positions before kk are restored, kk is perturbed
@@ -93,7 +104,17 @@ struct FdView {
     }
 };
 
-template <int FORM>
+// the same state when no restore residue exists: original except position kk
+struct FdCleanView {
+    const double *orig, *pert;
+    int kk;
+    __device__ __forceinline__ double operator()(int pos) const
+    {
+        return pos == kk ? pert[pos] : orig[pos];
+    }
+};
+
+template <int FORM, int SPEC>
 __global__ void __launch_bounds__(FD_THREADS) k_fd64(const ElemArgs a, const KParams prm)
 {
     __shared__ FdSmem sm;
@@ -125,10 +146,23 @@ __global__ void __launch_bounds__(FD_THREADS) k_fd64(const ElemArgs a, const KPa
             y[n] = a.xy[a.nnodes + gn];
         }
         auto go = geometry(c_bfn[ig], c_dfdc[ig], c_dfde[ig], c_d2fdc2[ig], c_d2fde2[ig],
-                             c_d2fdce[ig], c_w[ig], x, y, sm.dFx[el][ig], sm.dFy[el][ig],
-                             sm.d2x[el][ig], sm.d2y[el][ig]);
+                           c_d2fdce[ig], c_w[ig], x, y, sm.dFx[el][ig], sm.dFy[el][ig],
+                           sm.d2x[el][ig], sm.d2y[el][ig]);
         sm.H2[el][ig] = go.H2;
         sm.WET[el][ig] = go.WET;
+    }
+    __syncthreads();
+    if (live && k < 9) {
+        // interpolants of the original state, once per element and Gauss point
+        SmemView V0{sm.tl[el][0]};
+        sm.base[el][k] = interpolate(V0, c_bfn[k], sm.dFx[el][k], sm.dFy[el][k], sm.d2x[el][k],
+                                     sm.d2y[el][k]);
+    }
+    if (live && k == 9) {
+        int r = 0;
+        for (int i = 0; i < 54; i++)
+            r |= __double_as_longlong(sm.tl[el][1][i]) != __double_as_longlong(sm.tl[el][0][i]);
+        sm.residue[el] = r;
     }
     __syncthreads();
 
@@ -138,26 +172,40 @@ __global__ void __launch_bounds__(FD_THREADS) k_fd64(const ElemArgs a, const KPa
 #pragma unroll
     for (int i = 0; i < 54; i++) res[i] = 0.0;
     if (active) {
-        FdView V;
-        V.orig = sm.tl[el][0];
-        V.rest = sm.tl[el][1];
-        V.pert = sm.tl[el][2];
-        V.kk = (k == 0) ? -1 : (is_ac ? 54 : k - 1);
+        const int kk = (k == 0) ? -1 : (is_ac ? 54 : k - 1);
+        const int fk = kk >= 0 && kk < 54 ? kk - 6 * (kk / 6) : -1;
         double WiN = prm.WiN;
         if (prm.nex > 0) {
             const double eu = a.EU[prm.nex - 1];
             WiN = prm.Wi0 * (is_ac ? eu + eps : eu);
         }
+        const bool residue = sm.residue[el] != 0;
         for (int ig = 0; ig < 9; ig++) {
             const double *dFx = sm.dFx[el][ig], *dFy = sm.dFy[el][ig];
-            auto I = interpolate(V, c_bfn[ig], dFx, dFy, sm.d2x[el][ig], sm.d2y[el][ig]);
+            Interp<double> I;
+            if (!residue) {
+                // unperturbed fields from the cache; the perturbed field recomputed
+                I = sm.base[el][ig];
+                if (fk >= 0) {
+                    FdCleanView V{sm.tl[el][0], sm.tl[el][2], kk};
+                    interpolate_field(V, fk, c_bfn[ig], dFx, dFy, sm.d2x[el][ig], sm.d2y[el][ig],
+                                      I);
+                }
+            } else {
+                FdView V;
+                V.orig = sm.tl[el][0];
+                V.rest = sm.tl[el][1];
+                V.pert = sm.tl[el][2];
+                V.kk = kk;
+                I = interpolate(V, c_bfn[ig], dFx, dFy, sm.d2x[el][ig], sm.d2y[el][ig]);
+            }
             double dotU[9];
-            auto g = gauss_point<FORM>(I, prm, WiN, sm.H2[el][ig], dFx, dFy, dotU);
+            auto g = gauss_point<FORM, SPEC>(I, prm, WiN, sm.H2[el][ig], dFx, dFy, dotU);
             const double WET = sm.WET[el][ig];
 #pragma unroll
             for (int n = 0; n < 9; n++) {
                 double o[6];
-                test_node<FORM>(g, prm, c_bfn[ig][n], dFx[n], dFy[n], dotU[n], WET, o);
+                test_node<FORM, SPEC>(g, prm, c_bfn[ig][n], dFx[n], dFy[n], dotU[n], WET, o);
 #pragma unroll
                 for (int f = 0; f < 6; f++) res[n * 6 + f] = res[n * 6 + f] + o[f];
             }
@@ -192,11 +240,6 @@ __global__ void __launch_bounds__(FD_THREADS) k_fd64(const ElemArgs a, const KPa
 
 constexpr int RS_EPB = 8;
 constexpr int RS_THREADS = RS_EPB * 9;   // 72
-
-struct SmemView {
-    const double *p;
-    __device__ __forceinline__ double operator()(int pos) const { return p[pos]; }
-};
 
 template <int FORM>
 __global__ void __launch_bounds__(RS_THREADS) k_res64(const ElemArgs a, const KParams prm)
@@ -263,14 +306,26 @@ cudaError_t launch_residual64(const ElemArgs &a, const KParams &p, cudaStream_t 
     return cudaGetLastError();
 }
 
+template <int FORM>
+static void launch_fd64_form(const ElemArgs &a, const KParams &p, int grid, cudaStream_t s)
+{
+    const int spec = (p.ReN == 0.0 ? SPEC_RE0 : 0) | (p.DfN == 0.0 ? SPEC_DF0 : 0);
+    switch (spec) {
+    case 0: k_fd64<FORM, 0><<<grid, FD_THREADS, 0, s>>>(a, p); break;
+    case SPEC_RE0: k_fd64<FORM, SPEC_RE0><<<grid, FD_THREADS, 0, s>>>(a, p); break;
+    case SPEC_DF0: k_fd64<FORM, SPEC_DF0><<<grid, FD_THREADS, 0, s>>>(a, p); break;
+    default: k_fd64<FORM, SPEC_RE0 | SPEC_DF0><<<grid, FD_THREADS, 0, s>>>(a, p); break;
+    }
+}
+
 cudaError_t launch_fd64(const ElemArgs &a, const KParams &p, cudaStream_t s)
 {
     if (a.nel <= 0) return cudaSuccess;
     const int grid = (a.nel + FD_EPB - 1) / FD_EPB;
     if (p.form == FORM_SQRT)
-        k_fd64<FORM_SQRT><<<grid, FD_THREADS, 0, s>>>(a, p);
+        launch_fd64_form<FORM_SQRT>(a, p, grid, s);
     else
-        k_fd64<FORM_T><<<grid, FD_THREADS, 0, s>>>(a, p);
+        launch_fd64_form<FORM_T>(a, p, grid, s);
     return cudaGetLastError();
 }
 

@@ -47,9 +47,14 @@ struct ArrView {
     Cd operator()(int pos) const { return p[pos]; }
 };
 
-template <int FORM>
+// One element of the FD kernel (want_jac) or of the residual kernel, counted in
+// four parts: per-element work (state staging, geometry and, for the FD
+// kernel, the cached interpolants of the original state), one evaluation that
+// uses the cache (base and arclength evaluations), one evaluation that
+// recomputes its perturbed field, and one FD column of differences.
+template <int FORM, int SPEC>
 void count_element(const vefem::KParams &prm, const vefem::GaussTables &T, int want_jac,
-                   Tally *geo, Tally *evals, Tally *fdiff)
+                   Tally *once, Tally *ev_cached, Tally *ev_field, Tally *fdiff)
 {
     using namespace vefem;
     Cd x[9], y[9], tl[54];
@@ -59,8 +64,9 @@ void count_element(const vefem::KParams &prm, const vefem::GaussTables &T, int w
     }
     for (int i = 0; i < 54; i++) tl[i] = Cd(0.1 + 0.01 * i);
     Cd dFx[9][9], dFy[9][9], d2x[9][9], d2y[9][9], H2[9], WET[9];
-    // per element: state staging (x + eps, (x + eps) - eps) and geometry
-    g_tally = geo;
+    Interp<Cd> base[9];
+    ArrView V{tl};
+    g_tally = once;
     if (want_jac)
         for (int i = 0; i < 54; i++) {
             Cd vp = tl[i] + prm.eps;
@@ -72,29 +78,56 @@ void count_element(const vefem::KParams &prm, const vefem::GaussTables &T, int w
                            T.d2fdce[ig], T.w[ig], x, y, dFx[ig], dFy[ig], d2x[ig], d2y[ig]);
         H2[ig] = go.H2;
         WET[ig] = go.WET;
+        if (want_jac) base[ig] = interpolate(V, T.bfn[ig], dFx[ig], dFy[ig], d2x[ig], d2y[ig]);
     }
-    // one residual evaluation (all evaluations of an element cost the same)
-    g_tally = evals;
     Cd WiN = prm.nex > 0 ? prm.Wi0 * Cd(1.0) : Cd(prm.WiN);
-    Cd res[54];
-    ArrView V{tl};
-    for (int ig = 0; ig < 9; ig++) {
-        auto I = interpolate(V, T.bfn[ig], dFx[ig], dFy[ig], d2x[ig], d2y[ig]);
-        Cd dotU[9];
-        auto g = gauss_point<FORM>(I, prm, WiN, H2[ig], dFx[ig], dFy[ig], dotU);
-        for (int n = 0; n < 9; n++) {
-            Cd o[6];
-            test_node<FORM>(g, prm, T.bfn[ig][n], dFx[ig][n], dFy[ig][n], dotU[n], WET[ig], o);
-            for (int f = 0; f < 6; f++) res[n * 6 + f] = res[n * 6 + f] + o[f];
+    for (int pass = 0; pass < 2; pass++) {
+        g_tally = pass == 0 ? ev_cached : ev_field;
+        Cd res[54];
+        for (int ig = 0; ig < 9; ig++) {
+            Interp<Cd> I;
+            if (!want_jac)
+                I = interpolate(V, T.bfn[ig], dFx[ig], dFy[ig], d2x[ig], d2y[ig]);
+            else {
+                I = base[ig];
+                if (pass == 1) interpolate_field(V, 3, T.bfn[ig], dFx[ig], dFy[ig], d2x[ig], d2y[ig], I);
+            }
+            Cd dotU[9];
+            auto g = want_jac ? gauss_point<FORM, SPEC>(I, prm, WiN, H2[ig], dFx[ig], dFy[ig], dotU)
+                              : gauss_point<FORM>(I, prm, WiN, H2[ig], dFx[ig], dFy[ig], dotU);
+            for (int n = 0; n < 9; n++) {
+                Cd o[6];
+                if (want_jac)
+                    test_node<FORM, SPEC>(g, prm, T.bfn[ig][n], dFx[ig][n], dFy[ig][n], dotU[n],
+                                          WET[ig], o);
+                else
+                    test_node<FORM>(g, prm, T.bfn[ig][n], dFx[ig][n], dFy[ig][n], dotU[n],
+                                    WET[ig], o);
+                for (int f = 0; f < 6; f++) res[n * 6 + f] = res[n * 6 + f] + o[f];
+            }
+        }
+        if (pass == 0) {
+            g_tally = fdiff;
+            for (int i = 0; i < 54; i++) {
+                Cd d = (res[i] - res[i]) / prm.eps;
+                (void)d;
+            }
         }
     }
-    // one FD column: 54 differences divided by eps
-    g_tally = fdiff;
-    for (int i = 0; i < 54; i++) {
-        Cd d = (res[i] - res[i]) / prm.eps;
-        (void)d;
-    }
     g_tally = nullptr;
+}
+
+template <int FORM>
+void count_form(const vefem::KParams &k, const vefem::GaussTables &T, int want_jac, Tally *a,
+                Tally *b, Tally *c, Tally *d)
+{
+    const int spec = (k.ReN == 0.0 ? vefem::SPEC_RE0 : 0) | (k.DfN == 0.0 ? vefem::SPEC_DF0 : 0);
+    switch (spec) {
+    case 0: count_element<FORM, 0>(k, T, want_jac, a, b, c, d); break;
+    case 1: count_element<FORM, 1>(k, T, want_jac, a, b, c, d); break;
+    case 2: count_element<FORM, 2>(k, T, want_jac, a, b, c, d); break;
+    default: count_element<FORM, 3>(k, T, want_jac, a, b, c, d); break;
+    }
 }
 
 }  // namespace
@@ -112,20 +145,23 @@ extern "C" int vefem_algorithmic_ops(const vefem_params *p, int flags, double *o
     vefem::GaussTables T;
     vefem::gauss_tables_host(&T);
     const int want_jac = (flags & VEFEM_JAC_FD64) ? 1 : 0;
-    Tally geo, ev, fd;
+    Tally once, evc, evf, fd;
     if (p->form == 1)
-        count_element<1>(k, T, want_jac, &geo, &ev, &fd);
+        count_form<1>(k, T, want_jac, &once, &evc, &evf, &fd);
     else
-        count_element<0>(k, T, want_jac, &geo, &ev, &fd);
-    // evaluations per element: base (+ 54 columns + nex arclength columns)
-    const int64_t nev = want_jac ? 1 + 54 + p->nex : 1;
+        count_form<0>(k, T, want_jac, &once, &evc, &evf, &fd);
+    // FD kernel: base and arclength evaluations use the cached interpolants,
+    // the 54 column evaluations recompute one field; residual kernel: one
+    // evaluation with full interpolation (counted in the cached slot)
+    const int64_t nc = want_jac ? 1 + p->nex : 1;
+    const int64_t nf = want_jac ? 54 : 0;
     const int64_t ncol = want_jac ? 54 + p->nex : 0;
     Tally t;
-    t.add = geo.add + nev * ev.add + ncol * fd.add;
-    t.mul = geo.mul + nev * ev.mul + ncol * fd.mul;
-    t.div = geo.div + nev * ev.div + ncol * fd.div;
-    t.sqrt = geo.sqrt + nev * ev.sqrt + ncol * fd.sqrt;
-    t.exp = geo.exp + nev * ev.exp + ncol * fd.exp;
+    t.add = once.add + nc * evc.add + nf * evf.add + ncol * fd.add;
+    t.mul = once.mul + nc * evc.mul + nf * evf.mul + ncol * fd.mul;
+    t.div = once.div + nc * evc.div + nf * evf.div + ncol * fd.div;
+    t.sqrt = once.sqrt + nc * evc.sqrt + nf * evf.sqrt + ncol * fd.sqrt;
+    t.exp = once.exp + nc * evc.exp + nf * evf.exp + ncol * fd.exp;
     // Arclength column: eu + eps and Wi0 * eu once; residual-only: the in-order
     // Gauss-point sum is counted by the accumulation above.
     if (want_jac && p->nex) t.add += 1;

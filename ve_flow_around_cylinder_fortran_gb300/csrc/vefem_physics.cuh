@@ -23,6 +23,12 @@
 namespace vefem {
 
 enum { FORM_T = 0, FORM_SQRT = 1 };
+
+// Specialisations that leave out terms which are exact zeros for the given
+// parameters; a sum that drops an exact-zero addend keeps its value, so the
+// results are the same as the general code (up to the sign of a zero result).
+enum { SPEC_RE0 = 1,   // ReN == 0: convection, LSME-momentum and (ReN/dt, ReN*tsugn) terms
+       SPEC_DF0 = 2 }; // DfN == 0: stress diffusion terms and DfN/Helem^2
 enum { L_PTT = 0, M_L_PTT = 1, E_PTT = 2, M_E_PTT = 3, FENE_CR = 4, FENE_P = 5, GIESEKUS = 6 };
 
 // ---------------------------------------------------------------------------
@@ -141,13 +147,54 @@ VF_HD Interp<R> interpolate(const View &V, const double *bfn, const R *dFx, cons
     return I;
 }
 
+// Interpolants of one field f (value, x/y gradients, x/y second derivatives)
+// from a state accessor V(pos); the same sums, in the same order, as
+// interpolate() forms for that field.  Written into a copy of the cached
+// interpolants of the unperturbed state.
+template <class R, class View>
+VF_HD void interpolate_field(const View &V, int f, const double *bfn, const R *dFx, const R *dFy,
+                             const R *d2x, const R *d2y, Interp<R> &I)
+{
+    R val = 0.0, gx = 0.0, gy = 0.0, hx = 0.0, hy = 0.0;
+#pragma unroll
+    for (int n = 0; n < 9; n++) {
+        const R t = V(n * 6 + f);
+        val = val + t * bfn[n];
+        gx = gx + t * dFx[n];
+        gy = gy + t * dFy[n];
+        hx = hx + t * d2x[n];
+        hy = hy + t * d2y[n];
+    }
+    const R lap = hx + hy;
+    I.U1 = f == 0 ? val : I.U1;
+    I.GU11 = f == 0 ? gx : I.GU11;
+    I.GU21 = f == 0 ? gy : I.GU21;
+    I.lap1 = f == 0 ? lap : I.lap1;
+    I.U2 = f == 1 ? val : I.U2;
+    I.GU12 = f == 1 ? gx : I.GU12;
+    I.GU22 = f == 1 ? gy : I.GU22;
+    I.lap2 = f == 1 ? lap : I.lap2;
+    I.P = f == 2 ? val : I.P;
+    I.dPx = f == 2 ? gx : I.dPx;
+    I.dPy = f == 2 ? gy : I.dPy;
+    I.S11 = f == 3 ? val : I.S11;
+    I.dS11x = f == 3 ? gx : I.dS11x;
+    I.dS11y = f == 3 ? gy : I.dS11y;
+    I.S12 = f == 4 ? val : I.S12;
+    I.dS12x = f == 4 ? gx : I.dS12x;
+    I.dS12y = f == 4 ? gy : I.dS12y;
+    I.S22 = f == 5 ? val : I.S22;
+    I.dS22x = f == 5 ? gx : I.dS22x;
+    I.dS22y = f == 5 ? gy : I.dS22y;
+}
+
 // Strong form and stabilisation at a Gauss point:
 // strongFormEquations (:537-573), setFlowKinematics (:605-634), the
 // constitutive routines (Constitutive_Models_mod.F90, Constitutive_Models_SQRT_mod.F90),
 // strongFormMomentum/Continuity (:658-697), setStabilizationTerms (:701-773).
 // dotU[n] = U . grad(phi_n) is returned for reuse by the test-function loop
 // (the reference computes the same product there).
-template <int FORM, class R>
+template <int FORM, int SPEC = 0, class R>
 VF_HD GpCoef<R> gauss_point(const Interp<R> &I, const KParams &prm, R WiN, R H2, const R *dFx,
                             const R *dFy, R *dotU)
 {
@@ -343,10 +390,17 @@ VF_HD GpCoef<R> gauss_point(const Interp<R> &I, const KParams &prm, R WiN, R H2,
     const R divP2 = (-I.dPy + divT2) + BvN * I.lap2;
     const R conv1 = I.U1 * I.GU11 + I.U2 * I.GU21;
     const R conv2 = I.U1 * I.GU12 + I.U2 * I.GU22;
-    g.rc1 = ReN * conv1;
-    g.rc2 = ReN * conv2;
-    g.M1 = g.rc1 - divP1;
-    g.M2 = g.rc2 - divP2;
+    if (SPEC & SPEC_RE0) {
+        g.rc1 = 0.0;
+        g.rc2 = 0.0;
+        g.M1 = -divP1;
+        g.M2 = -divP2;
+    } else {
+        g.rc1 = ReN * conv1;
+        g.rc2 = ReN * conv2;
+        g.M1 = g.rc1 - divP1;
+        g.M2 = g.rc2 - divP2;
+    }
     g.Cont = tr;
     // setStabilizationTerms :701-773
     R tsugn = 0.0;
@@ -360,12 +414,18 @@ VF_HD GpCoef<R> gauss_point(const Interp<R> &I, const KParams &prm, R WiN, R H2,
     const R r = omb / WiN;
     R Ha = sqrt(r * r + 0.5 * ddT);
     Ha = Ha / sqrt(1.0 + 0.5 * ddG);
-    const R a1 = ReN / prm.dt, a2 = ReN * tsugn, a3 = BvN / H2, a4 = Ha / H2;
-    R tlsme = a1 * a1 + a2 * a2 + a3 * a3 + a4 * a4;
+    const R a3 = BvN / H2, a4 = Ha / H2;
+    R tlsme;
+    if (SPEC & SPEC_RE0) {
+        tlsme = a3 * a3 + a4 * a4;
+    } else {
+        const R a1 = ReN / prm.dt, a2 = ReN * tsugn;
+        tlsme = a1 * a1 + a2 * a2 + a3 * a3 + a4 * a4;
+    }
     tlsme = 1.0 / sqrt(tlsme);
     g.tlsme = tlsme;
     g.tlsic = H2 / tlsme;
-    g.tR = tlsme * ReN;
+    if (!(SPEC & SPEC_RE0)) g.tR = tlsme * ReN;
     R tdcs = 0.5 * ddS;
     if (FORM == FORM_T) tdcs = tdcs + r * r;
     tdcs = H2 / sqrt(tdcs);
@@ -375,8 +435,12 @@ VF_HD GpCoef<R> gauss_point(const Interp<R> &I, const KParams &prm, R WiN, R H2,
     mag = sqrt(0.5 * mag);
     g.mag = mag;
     const R b1 = WiN / prm.dt, b2 = WiN * tsugn, b3 = WiN * sqrt(0.5 * ddG), b4 = f2;
-    const R b5 = f3 * sqrt(0.5 * ddC), b6 = tdcs * mag / H2, b7 = DfN / H2;
-    R tlsce = b1 * b1 + b2 * b2 + b3 * b3 + b4 * b4 + b5 * b5 + b6 * b6 + b7 * b7;
+    const R b5 = f3 * sqrt(0.5 * ddC), b6 = tdcs * mag / H2;
+    R tlsce = b1 * b1 + b2 * b2 + b3 * b3 + b4 * b4 + b5 * b5 + b6 * b6;
+    if (!(SPEC & SPEC_DF0)) {
+        const R b7 = DfN / H2;
+        tlsce = tlsce + b7 * b7;
+    }
     tlsce = 1.0 / sqrt(tlsce);
     g.tlsce = tlsce;
     g.ntl = -tlsce;
@@ -385,14 +449,18 @@ VF_HD GpCoef<R> gauss_point(const Interp<R> &I, const KParams &prm, R WiN, R H2,
 
 // Weak-form terms of one test node n (momentumMain(SQRT), continuityBulkMain,
 // stressesBulkMain(SQRT), Residuals_mod.F90:44-157, 295-490) times WET.
-template <int FORM, class R, class Out>
+template <int FORM, int SPEC = 0, class R, class Out>
 VF_HD void test_node(const GpCoef<R> &g, const KParams &prm, double bifn, R fx, R fy, R du,
                      R WET, Out *out)
 {
     const R DfN = prm.DfN;
     // momentum
-    const R lme = g.tR * du;
-    const R lsme1 = lme * g.M1, lsme2 = lme * g.M2;
+    R lsme1, lsme2;
+    if (!(SPEC & SPEC_RE0)) {
+        const R lme = g.tR * du;
+        lsme1 = lme * g.M1;
+        lsme2 = lme * g.M2;
+    }
     const R lsic1 = (g.tlsic * fx) * g.Cont, lsic2 = (g.tlsic * fy) * g.Cont;
     R lsce1, lsce2;
     if (FORM == FORM_T) {
@@ -426,8 +494,14 @@ VF_HD void test_node(const GpCoef<R> &g, const KParams &prm, double bifn, R fx, 
     }
     const R pd1 = g.P11 * fx + g.P12 * fy;
     const R pd2 = g.P12 * fx + g.P22 * fy;
-    const R t0 = (((g.rc1 * bifn + pd1) + lsme1) + lsic1) + lsce1;
-    const R t1 = (((g.rc2 * bifn + pd2) + lsme2) + lsic2) + lsce2;
+    R t0, t1;
+    if (SPEC & SPEC_RE0) {
+        t0 = (pd1 + lsic1) + lsce1;
+        t1 = (pd2 + lsic2) + lsce2;
+    } else {
+        t0 = (((g.rc1 * bifn + pd1) + lsme1) + lsic1) + lsce1;
+        t1 = (((g.rc2 * bifn + pd2) + lsme2) + lsic2) + lsce2;
+    }
     // continuity
     const R t2 = g.Cont * bifn + g.tlsme * (fx * g.M1 + fy * g.M2);
     // stresses (j,k) = (1,1), (1,2), (2,2)
@@ -449,9 +523,16 @@ VF_HD void test_node(const GpCoef<R> &g, const KParams &prm, double bifn, R fx, 
         ls22 = g.tlsme * ls22 * g.WiN;
         lce = g.tlsce * (g.WiN * du + g.fT * bifn / 2.0);
     }
-    const R t3 = (((g.C11 * bifn + DfN * gd11) + ls11) + lce * g.C11) + (g.tdcs * gd11) * g.mag;
-    const R t4 = (((g.C12 * bifn + DfN * gd12) + ls12) + lce * g.C12) + (g.tdcs * gd12) * g.mag;
-    const R t5 = (((g.C22 * bifn + DfN * gd22) + ls22) + lce * g.C22) + (g.tdcs * gd22) * g.mag;
+    R t3, t4, t5;
+    if (SPEC & SPEC_DF0) {
+        t3 = ((g.C11 * bifn + ls11) + lce * g.C11) + (g.tdcs * gd11) * g.mag;
+        t4 = ((g.C12 * bifn + ls12) + lce * g.C12) + (g.tdcs * gd12) * g.mag;
+        t5 = ((g.C22 * bifn + ls22) + lce * g.C22) + (g.tdcs * gd22) * g.mag;
+    } else {
+        t3 = (((g.C11 * bifn + DfN * gd11) + ls11) + lce * g.C11) + (g.tdcs * gd11) * g.mag;
+        t4 = (((g.C12 * bifn + DfN * gd12) + ls12) + lce * g.C12) + (g.tdcs * gd12) * g.mag;
+        t5 = (((g.C22 * bifn + DfN * gd22) + ls22) + lce * g.C22) + (g.tdcs * gd22) * g.mag;
+    }
     out[0] = t0 * WET;
     out[1] = t1 * WET;
     out[2] = t2 * WET;
