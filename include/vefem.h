@@ -65,6 +65,10 @@ extern "C" {
 #define VEFEM_RESIDUAL 0x1       /* add the element residuals into b ('MNR' and 'NRP') */
 #define VEFEM_JAC_FD64 0x2       /* add the FP64 forward-difference Jacobian ('NRP'),
                                     the reference algorithm of storeBulk, bit-exact */
+#define VEFEM_JAC_EXACT64 0x4    /* add the exact (linearised) Jacobian in FP64: forward-mode
+                                    derivative of the same physics, no FD truncation error */
+#define VEFEM_JAC_EXACT32 0x8    /* the exact Jacobian in FP32 into a float AIJ values array:
+                                    the inexact-Newton precision form (residual stays FP64) */
 #define VEFEM_ZERO_FIRST 0x100   /* zero b (and vals when a Jacobian is requested) before
                                     adding, like initializeLSObjects (Petsc_mod.F90:747-763) */
 #define VEFEM_OUTLET_EDGES 0x200 /* also add the outlet open-BC edge terms (openBC,
@@ -118,14 +122,17 @@ int vefem_create(const vefem_mesh *mesh, const vefem_csr *pattern, const vefem_p
 int vefem_set_params(vefem_ctx *ctx, const vefem_params *params);
 
 /* One bulk assembly: setEquationsBulk with Flag_NR = 'MNR' (VEFEM_RESIDUAL)
- * or 'NRP' (VEFEM_RESIDUAL | VEFEM_JAC_FD64).
+ * or 'NRP' (VEFEM_RESIDUAL | one Jacobian flag: VEFEM_JAC_FD64 is the
+ * reference's algorithm; VEFEM_JAC_EXACT64 / VEFEM_JAC_EXACT32 the exact
+ * derivative in FP64 / FP32).
  * on_device = 0: TL, EU, b, vals are host pointers (copied in and out;
  *                pinned memory gives full link speed);
  * on_device = 1: they are device pointers (CUDA unified addressing).
- * vals is double[nnz] and may be NULL when no Jacobian is requested.
- * The call returns when the results are in b and vals. */
+ * vals is double[nnz] (float[nnz] with VEFEM_JAC_EXACT32) and may be NULL
+ * when no Jacobian is requested.  Outlet edges (VEFEM_OUTLET_EDGES) always
+ * use the FD Jacobian.  The call returns when the results are in b and vals. */
 int vefem_assemble(vefem_ctx *ctx, const double *TL, const double *EU, int flags, double *b,
-                   double *vals, int on_device);
+                   void *vals, int on_device);
 
 /* Per-kernel times (milliseconds, CUDA events on the context's stream) of the
  * last vefem_assemble called with VEFEM_TIMING:

@@ -21,7 +21,9 @@ PROBE = os.path.join(OUT, "libvefem_probe.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 SOURCES = ["vefem_fd64.cu", "vefem_gather.cu", "vefem_capi.cu", "vefem_opcount.cpp",
-           "vefem_noalloc.cu"]
+           "vefem_noalloc.cu", "vefem_exact.cu"]
+# the exact-Jacobian kernels are not held to bit-exactness: FMA contraction allowed
+FMAD_ON = {"vefem_exact.cu"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -32,8 +34,9 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found")
 
 
-def _flags():
-    return ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
+def _flags(src: str = ""):
+    fmad = "-fmad=true" if src in FMAD_ON else "-fmad=false"
+    return ARCH + ["-O3", "-lineinfo", "-std=c++17", fmad, "-Xcompiler", "-fPIC",
                    "-Xcompiler", "-ffp-contract=off", "-I", INCLUDE, "-I", CSRC]
 
 
@@ -61,7 +64,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     for src in SOURCES:
         obj = os.path.join(OUT, os.path.splitext(src)[0] + ".o")
         objs.append(obj)
-        cmd = [cc] + _flags() + (["-Xptxas", "-v"] if verbose else []) + \
+        cmd = [cc] + _flags(src) + (["-Xptxas", "-v"] if verbose else []) + \
             ["-c", os.path.join(CSRC, src), "-o", obj]
         procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
     failed = False

@@ -48,6 +48,8 @@ struct vefem_ctx {
     int32_t *d_edge_row = nullptr, *d_edge_off = nullptr;   // [nedge][81]
     // device scratch / staging (allocated on first use)
     double *d_rs = nullptr, *d_es = nullptr, *d_as = nullptr;
+    float *d_es32 = nullptr, *d_as32 = nullptr;
+    float *d_vals32 = nullptr;
     double *d_ers = nullptr, *d_ees = nullptr, *d_eas = nullptr;
     double *d_TL = nullptr, *d_EU = nullptr, *d_b = nullptr, *d_vals = nullptr;
 };
@@ -155,10 +157,11 @@ void gauss_tables_host(GaussTables *t)
 }
 
 // edge contributions, sequential over edges (setEquationsEdge runs after the bulk)
+template <class V>
 __global__ void k_gather_edges(int nedge, int nex, const int64_t *rowptr, const int32_t *conn,
                                int nel, const int32_t *edge_elem, const int32_t *edge_row,
                                const int32_t *edge_off, const double *rs, const double *es,
-                               const double *as, double *b, double *vals, int want_jac)
+                               const double *as, double *b, V *vals, int want_jac)
 {
     for (int k = 0; k < nedge; k++) {
         const int e = edge_elem[k];
@@ -175,14 +178,14 @@ __global__ void k_gather_edges(int nedge, int nex, const int64_t *rowptr, const 
                 const int jeq = q / 6, ieq = q - 6 * (q / 6);
                 const int64_t slot = rowptr[(int64_t)edge_row[k * 81 + blk] * 6 + jeq] +
                                      edge_off[k * 81 + blk] + ieq;
-                vals[slot] = vals[slot] + es[(int64_t)k * 2916 + r];
+                vals[slot] = vals[slot] + (V)es[(int64_t)k * 2916 + r];
             } else {
                 if (!want_jac || nex == 0) continue;
                 const int r = t - 54 - 2916;
                 const int jnod = r / 6, jeq = r - 6 * (r / 6);
                 const int64_t row = (int64_t)conn[jnod * nel + e] * 6 + jeq;
                 const int64_t slot = rowptr[row + 1] - 1;
-                vals[slot] = vals[slot] + as[(int64_t)k * 54 + r];
+                vals[slot] = vals[slot] + (V)as[(int64_t)k * 54 + r];
             }
         }
         __syncthreads();
@@ -444,7 +447,8 @@ extern "C" int vefem_create(const vefem_mesh *mesh, const vefem_csr *pat,
         UPL(d_edge_off, eoff.data(), eoff.size())
     }
 #undef UPL
-    if ((ce = upload_tables(tab, s)) != cudaSuccess || (ce = cudaStreamSynchronize(s)) != cudaSuccess) {
+    if ((ce = upload_tables(tab, s)) != cudaSuccess || (ce = upload_tables_exact(tab, s)) != cudaSuccess ||
+        (ce = cudaStreamSynchronize(s)) != cudaSuccess) {
         std::string m = std::string("tables: ") + cudaGetErrorString(ce);
         vefem_destroy(ctx);
         return fail(nullptr, VEFEM_ERR_CUDA, m);
@@ -471,21 +475,28 @@ static cudaError_t ensure(double **p, size_t n)
 }
 
 extern "C" int vefem_assemble(vefem_ctx *ctx, const double *TL, const double *EU, int flags,
-                              double *b, double *vals, int on_device)
+                              double *b, void *vals_v, int on_device)
 {
     if (!ctx) return VEFEM_ERR_ARG;
-    const int known = VEFEM_RESIDUAL | VEFEM_JAC_FD64 | VEFEM_ZERO_FIRST | VEFEM_OUTLET_EDGES |
-                      VEFEM_TIMING;
+    const int known = VEFEM_RESIDUAL | VEFEM_JAC_FD64 | VEFEM_JAC_EXACT64 | VEFEM_JAC_EXACT32 |
+                      VEFEM_ZERO_FIRST | VEFEM_OUTLET_EDGES | VEFEM_TIMING;
     if (flags & ~known) return fail(ctx, VEFEM_ERR_UNSUPPORTED, "unknown flag");
+    const int jmode = flags & (VEFEM_JAC_FD64 | VEFEM_JAC_EXACT64 | VEFEM_JAC_EXACT32);
+    if (jmode && (jmode & (jmode - 1)))
+        return fail(ctx, VEFEM_ERR_ARG, "at most one Jacobian flag");
     const bool want_res = flags & VEFEM_RESIDUAL;
-    const bool want_jac = flags & VEFEM_JAC_FD64;
+    const bool want_jac = jmode != 0;
+    const bool jac32 = jmode == VEFEM_JAC_EXACT32;
+    const size_t vsize = jac32 ? sizeof(float) : sizeof(double);
+    double *vals = jac32 ? nullptr : static_cast<double *>(vals_v);
+    float *vals32 = jac32 ? static_cast<float *>(vals_v) : nullptr;
     const bool edges = (flags & VEFEM_OUTLET_EDGES) && ctx->nedge > 0;
     const bool timing = flags & VEFEM_TIMING;
     if (!want_res && !want_jac) return fail(ctx, VEFEM_ERR_ARG, "nothing requested");
     if (!TL) return fail(ctx, VEFEM_ERR_ARG, "TL is NULL");
     if (ctx->nex > 0 && !EU) return fail(ctx, VEFEM_ERR_ARG, "EU is NULL with nex = 1");
     if (want_res && !b) return fail(ctx, VEFEM_ERR_ARG, "b is NULL");
-    if (want_jac && !vals) return fail(ctx, VEFEM_ERR_ARG, "vals is NULL");
+    if (want_jac && !vals_v) return fail(ctx, VEFEM_ERR_ARG, "vals is NULL");
     CK(cudaSetDevice(ctx->device));
     cudaStream_t s = ctx->stream;
     const size_t nel = ctx->nel, nn = ctx->nnodes;
@@ -493,9 +504,13 @@ extern "C" int vefem_assemble(vefem_ctx *ctx, const double *TL, const double *EU
     for (int i = 0; i < 5; i++) ctx->timing[i] = 0.0f;
 
     CK(ensure(&ctx->d_rs, nel * 54));
-    if (want_jac) {
+    if (want_jac && !jac32) {
         CK(ensure(&ctx->d_es, nel * 2916));
         if (ctx->nex) CK(ensure(&ctx->d_as, nel * 54));
+    }
+    if (jac32) {
+        if (!ctx->d_es32) CK(cudaMalloc((void **)&ctx->d_es32, nel * 2916 * sizeof(float)));
+        if (ctx->nex && !ctx->d_as32) CK(cudaMalloc((void **)&ctx->d_as32, nel * 54 * sizeof(float)));
     }
     if (edges) {
         CK(ensure(&ctx->d_ers, (size_t)ctx->nedge * 54));
@@ -504,6 +519,7 @@ extern "C" int vefem_assemble(vefem_ctx *ctx, const double *TL, const double *EU
     }
     const double *dTL = TL, *dEU = EU;
     double *db = b, *dvals = vals;
+    float *dvals32 = vals32;
     if (timing) CK(cudaEventRecord(ctx->ev[0], s));
     if (!on_device) {
         CK(ensure(&ctx->d_TL, nn * 6));
@@ -520,16 +536,22 @@ extern "C" int vefem_assemble(vefem_ctx *ctx, const double *TL, const double *EU
             if (!(flags & VEFEM_ZERO_FIRST))
                 CK(cudaMemcpyAsync(db, b, ctx->N * sizeof(double), cudaMemcpyHostToDevice, s));
         }
-        if (want_jac) {
+        if (want_jac && !jac32) {
             CK(ensure(&ctx->d_vals, (size_t)ctx->nnz));
             dvals = ctx->d_vals;
             if (!(flags & VEFEM_ZERO_FIRST))
                 CK(cudaMemcpyAsync(dvals, vals, ctx->nnz * sizeof(double), cudaMemcpyHostToDevice, s));
         }
+        if (jac32) {
+            if (!ctx->d_vals32) CK(cudaMalloc((void **)&ctx->d_vals32, ctx->nnz * sizeof(float)));
+            dvals32 = ctx->d_vals32;
+            if (!(flags & VEFEM_ZERO_FIRST))
+                CK(cudaMemcpyAsync(dvals32, vals32, ctx->nnz * sizeof(float), cudaMemcpyHostToDevice, s));
+        }
     }
     if (flags & VEFEM_ZERO_FIRST) {
         if (want_res) CK(cudaMemsetAsync(db, 0, ctx->N * sizeof(double), s));
-        if (want_jac) CK(cudaMemsetAsync(dvals, 0, ctx->nnz * sizeof(double), s));
+        if (want_jac) CK(cudaMemsetAsync(jac32 ? (void *)dvals32 : (void *)dvals, 0, ctx->nnz * vsize, s));
     }
     if (timing) CK(cudaEventRecord(ctx->ev[1], s));
 
@@ -543,11 +565,22 @@ extern "C" int vefem_assemble(vefem_ctx *ctx, const double *TL, const double *EU
     ea.rs = ctx->d_rs;
     ea.es = ctx->d_es;
     ea.as = ctx->d_as;
-    if (want_jac)
+    if (jmode == VEFEM_JAC_FD64) {
         CK(launch_fd64(ea, ctx->prm, s));
-    else
-        CK(launch_residual64(ea, ctx->prm, s));
-    ctx->launches++;
+        ctx->launches++;
+    } else {
+        if (want_res) {
+            CK(launch_residual64(ea, ctx->prm, s));
+            ctx->launches++;
+        }
+        if (jmode == VEFEM_JAC_EXACT64) {
+            CK(launch_exact<double>(ea, ctx->prm, ctx->d_es, ctx->d_as, s));
+            ctx->launches++;
+        } else if (jac32) {
+            CK(launch_exact<float>(ea, ctx->prm, ctx->d_es32, ctx->d_as32, s));
+            ctx->launches++;
+        }
+    }
     if (timing) CK(cudaEventRecord(ctx->ev[2], s));
 
     GatherArgs ga;
@@ -566,11 +599,19 @@ extern "C" int vefem_assemble(vefem_ctx *ctx, const double *TL, const double *EU
         ctx->launches++;
     }
     if (timing) CK(cudaEventRecord(ctx->ev[3], s));
-    if (want_jac) {
+    if (want_jac && !jac32) {
         CK(launch_gather_jacobian(ga, ctx->d_es, dvals, s));
         ctx->launches++;
         if (ctx->nex) {
             CK(launch_gather_arclength(ga, ctx->d_as, dvals, s));
+            ctx->launches++;
+        }
+    }
+    if (jac32) {
+        CK(launch_gather_jacobian32(ga, ctx->d_es32, dvals32, s));
+        ctx->launches++;
+        if (ctx->nex) {
+            CK(launch_gather_arclength32(ga, ctx->d_as32, dvals32, s));
             ctx->launches++;
         }
     }
@@ -590,11 +631,16 @@ extern "C" int vefem_assemble(vefem_ctx *ctx, const double *TL, const double *EU
         eg.es = ctx->d_ees;
         eg.as = ctx->d_eas;
         CK(launch_edge64(eg, ctx->prm, want_jac ? 1 : 0, s));
-        k_gather_edges<<<1, 1024, 0, s>>>(ctx->nedge, ctx->nex, ctx->d_rowptr, ctx->d_conn,
-                                          ctx->nel, ctx->d_edge_elem, ctx->d_edge_row,
-                                          ctx->d_edge_off, ctx->d_ers, ctx->d_ees, ctx->d_eas,
-                                          want_res ? db : nullptr, want_jac ? dvals : nullptr,
-                                          want_jac ? 1 : 0);
+        if (jac32)
+            k_gather_edges<float><<<1, 1024, 0, s>>>(
+                ctx->nedge, ctx->nex, ctx->d_rowptr, ctx->d_conn, ctx->nel, ctx->d_edge_elem,
+                ctx->d_edge_row, ctx->d_edge_off, ctx->d_ers, ctx->d_ees, ctx->d_eas,
+                want_res ? db : nullptr, dvals32, 1);
+        else
+            k_gather_edges<double><<<1, 1024, 0, s>>>(
+                ctx->nedge, ctx->nex, ctx->d_rowptr, ctx->d_conn, ctx->nel, ctx->d_edge_elem,
+                ctx->d_edge_row, ctx->d_edge_off, ctx->d_ers, ctx->d_ees, ctx->d_eas,
+                want_res ? db : nullptr, want_jac ? dvals : nullptr, want_jac ? 1 : 0);
         CK(cudaGetLastError());
         ctx->launches += 2;
     }
@@ -602,8 +648,10 @@ extern "C" int vefem_assemble(vefem_ctx *ctx, const double *TL, const double *EU
     if (!on_device) {
         if (want_res)
             CK(cudaMemcpyAsync(b, db, ctx->N * sizeof(double), cudaMemcpyDeviceToHost, s));
-        if (want_jac)
+        if (want_jac && !jac32)
             CK(cudaMemcpyAsync(vals, dvals, ctx->nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
+        if (jac32)
+            CK(cudaMemcpyAsync(vals32, dvals32, ctx->nnz * sizeof(float), cudaMemcpyDeviceToHost, s));
     }
     if (timing) CK(cudaEventRecord(ctx->ev[6], s));
     CK(cudaStreamSynchronize(s));
@@ -644,7 +692,7 @@ extern "C" int vefem_destroy(vefem_ctx *ctx)
                     ctx->d_boff, ctx->d_bptr, ctx->d_bcon, ctx->d_edge_elem, ctx->d_edge_id,
                     ctx->d_edge_row, ctx->d_edge_off, ctx->d_rs, ctx->d_es, ctx->d_as,
                     ctx->d_ers, ctx->d_ees, ctx->d_eas, ctx->d_TL, ctx->d_EU, ctx->d_b,
-                    ctx->d_vals};
+                    ctx->d_vals, ctx->d_es32, ctx->d_as32, ctx->d_vals32};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int i = 0; i < 8; i++)

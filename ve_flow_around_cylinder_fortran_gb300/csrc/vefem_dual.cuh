@@ -1,0 +1,75 @@
+// Forward-mode dual number with one tangent direction, used to differentiate
+// the Gauss-point physics (vefem_physics.cuh) for the exact Jacobian.
+// sqrt and fabs take the derivative 0 at 0 (a subgradient), where the
+// classical derivative does not exist.
+#pragma once
+
+#include <math.h>
+
+#ifdef __CUDACC__
+#define VD_HD __host__ __device__ __forceinline__
+#else
+#define VD_HD inline
+#endif
+
+namespace vefem {
+
+// plain overloads: the Dual templates below would otherwise hide the global
+// math functions from unqualified calls inside this namespace
+VD_HD double sqrt(double x) { return ::sqrt(x); }
+VD_HD float sqrt(float x) { return ::sqrtf(x); }
+VD_HD double exp(double x) { return ::exp(x); }
+VD_HD float exp(float x) { return ::expf(x); }
+VD_HD double fabs(double x) { return ::fabs(x); }
+VD_HD float fabs(float x) { return ::fabsf(x); }
+
+template <class T>
+struct Dual {
+    T v, d;
+    VD_HD Dual() : v(0), d(0) {}
+    VD_HD Dual(double x) : v((T)x), d(0) {}
+    VD_HD Dual(T x, T dx) : v(x), d(dx) {}
+};
+
+template <class T> VD_HD Dual<T> operator+(Dual<T> a, Dual<T> b) { return Dual<T>(a.v + b.v, a.d + b.d); }
+template <class T> VD_HD Dual<T> operator-(Dual<T> a, Dual<T> b) { return Dual<T>(a.v - b.v, a.d - b.d); }
+template <class T> VD_HD Dual<T> operator*(Dual<T> a, Dual<T> b)
+{
+    return Dual<T>(a.v * b.v, a.d * b.v + a.v * b.d);
+}
+template <class T> VD_HD Dual<T> operator/(Dual<T> a, Dual<T> b)
+{
+    const T q = a.v / b.v;
+    return Dual<T>(q, (a.d - q * b.d) / b.v);
+}
+template <class T> VD_HD Dual<T> operator-(Dual<T> a) { return Dual<T>(-a.v, -a.d); }
+
+template <class T> VD_HD Dual<T> operator+(Dual<T> a, double b) { return Dual<T>(a.v + (T)b, a.d); }
+template <class T> VD_HD Dual<T> operator-(Dual<T> a, double b) { return Dual<T>(a.v - (T)b, a.d); }
+template <class T> VD_HD Dual<T> operator*(Dual<T> a, double b) { return Dual<T>(a.v * (T)b, a.d * (T)b); }
+template <class T> VD_HD Dual<T> operator/(Dual<T> a, double b) { return Dual<T>(a.v / (T)b, a.d / (T)b); }
+template <class T> VD_HD Dual<T> operator+(double a, Dual<T> b) { return Dual<T>((T)a + b.v, b.d); }
+template <class T> VD_HD Dual<T> operator-(double a, Dual<T> b) { return Dual<T>((T)a - b.v, -b.d); }
+template <class T> VD_HD Dual<T> operator*(double a, Dual<T> b) { return Dual<T>((T)a * b.v, (T)a * b.d); }
+template <class T> VD_HD Dual<T> operator/(double a, Dual<T> b)
+{
+    const T q = (T)a / b.v;
+    return Dual<T>(q, -q * b.d / b.v);
+}
+
+template <class T> VD_HD Dual<T> sqrt(Dual<T> a)
+{
+    const T r = sqrt(a.v);
+    return Dual<T>(r, r > (T)0 ? a.d / (r + r) : (T)0);
+}
+template <class T> VD_HD Dual<T> exp(Dual<T> a)
+{
+    const T e = exp(a.v);
+    return Dual<T>(e, e * a.d);
+}
+template <class T> VD_HD Dual<T> fabs(Dual<T> a)
+{
+    return Dual<T>(fabs(a.v), a.v > (T)0 ? a.d : (a.v < (T)0 ? -a.d : (T)0));
+}
+
+}  // namespace vefem

@@ -1,0 +1,273 @@
+// Exact (linearised) element Jacobian by forward-mode differentiation of the
+// Gauss-point physics, in FP32 (the inexact-Newton "precision form") or FP64.
+//
+// At a Gauss point the weak-form term of test node i and equation e is linear
+// in the test function: TERM(i,e) = sum_k c_ek(q) psi_k(i), psi = (phi, dphi/dx,
+// dphi/dy), where the coefficients c (6 equations x 3) depend on the 20
+// interpolated quantities q (u, v: value, x/y gradient, Laplacian; p and the
+// three stress components: value, x/y gradient) and on Wi (through the
+// arclength unknown).  Each unknown x(j,f) enters q linearly through chi(j) =
+// (phi_j, dphi_j/dx, dphi_j/dy, Laplacian phi_j).  Hence
+//     dR(i,e)/dx(j,f) = sum_gp WET sum_k psi_k(i) sum_s (dc_ek/dq_fs) chi_s(j).
+// The kernel gets dc/dq with 21 one-direction dual evaluations per Gauss
+// point (the kernels' own physics source with R = Dual<T>), then contracts.
+// This replaces the 56 residual evaluations of the forward difference; it is
+// the derivative the FD approximates (they differ by the FD truncation error).
+//
+// One CTA per element, 192 threads:
+//   phase 0  state and geometry (geometry in FP64, stored in T);
+//   phase 1  thread (gp, d): D[gp][d][e*3+k] = dc_ek/dq_d;
+//   phase 2a A[gp][d][i*6+e] = WET sum_k psi_k(i) D[gp][d][e*3+k];
+//   phase 2b K(i,e; j,f) = sum_gp sum_s A[gp][q(f,s)][i*6+e] chi_s(j), and the
+//            arclength column sum_gp A[gp][20][i*6+e];
+// written to the element scratch in the block layout the scatter reads.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "vefem_dual.cuh"
+#include "vefem_internal.h"
+#include "vefem_physics.cuh"
+
+namespace vefem {
+
+__constant__ double x_w[9];
+__constant__ double x_bfn[9][9];
+__constant__ double x_dfdc[9][9];
+__constant__ double x_dfde[9][9];
+__constant__ double x_d2fdc2[9][9];
+__constant__ double x_d2fde2[9][9];
+__constant__ double x_d2fdce[9][9];
+
+cudaError_t upload_tables_exact(const GaussTables &t, cudaStream_t s)
+{
+    cudaError_t e = cudaSuccess;
+#define UP(sym, src)                                                                       \
+    if (e == cudaSuccess)                                                                  \
+        e = cudaMemcpyToSymbolAsync(sym, src, sizeof(src), 0, cudaMemcpyHostToDevice, s);
+    UP(x_w, t.w)
+    UP(x_bfn, t.bfn)
+    UP(x_dfdc, t.dfdc)
+    UP(x_dfde, t.dfde)
+    UP(x_d2fdc2, t.d2fdc2)
+    UP(x_d2fde2, t.d2fde2)
+    UP(x_d2fdce, t.d2fdce)
+#undef UP
+    return e;
+}
+
+constexpr int EX_THREADS = 192;
+constexpr int EX_NDIR = 21;      // 20 interpolated quantities + the arclength unknown
+
+// direction index of quantity s (0 value, 1 d/dx, 2 d/dy, 3 Laplacian) of field f
+__device__ __forceinline__ int qdir(int f, int s)
+{
+    return f == 0 ? s : (f == 1 ? 4 + s : 8 + 3 * (f - 2) + s);
+}
+
+template <class T>
+struct TView {
+    const T *p;
+    __device__ __forceinline__ T operator()(int pos) const { return p[pos]; }
+};
+
+template <class T, int FORM, int SPEC>
+__global__ void __launch_bounds__(EX_THREADS)
+k_exact(const ElemArgs a, const KParams prm, T *__restrict__ es, T *__restrict__ as)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T *D = reinterpret_cast<T *>(smraw);               // [9][21][18]
+    T *A = D + 9 * EX_NDIR * 18;                       // [9][21][54]
+    __shared__ T s_tl[54];
+    __shared__ T s_dFx[9][9], s_dFy[9][9], s_d2x[9][9], s_d2y[9][9], s_lap[9][9];
+    __shared__ T s_H2[9], s_WET[9];
+    const int e = blockIdx.x;
+    const int t = threadIdx.x;
+
+    if (t < 54) {
+        const int inod = t / 6, f = t - 6 * (t / 6);
+        s_tl[t] = (T)a.TL[(size_t)f * a.nnodes + a.conn[inod * a.nel + e]];
+    } else if (t >= 64 && t < 73) {
+        const int ig = t - 64;
+        double x[9], y[9], fx[9], fy[9], sx[9], sy[9];
+#pragma unroll
+        for (int n = 0; n < 9; n++) {
+            const int gn = a.conn[n * a.nel + e];
+            x[n] = a.xy[gn];
+            y[n] = a.xy[a.nnodes + gn];
+        }
+        auto go = geometry(x_bfn[ig], x_dfdc[ig], x_dfde[ig], x_d2fdc2[ig], x_d2fde2[ig],
+                           x_d2fdce[ig], x_w[ig], x, y, fx, fy, sx, sy);
+#pragma unroll
+        for (int n = 0; n < 9; n++) {
+            s_dFx[ig][n] = (T)fx[n];
+            s_dFy[ig][n] = (T)fy[n];
+            s_d2x[ig][n] = (T)sx[n];
+            s_d2y[ig][n] = (T)sy[n];
+            s_lap[ig][n] = (T)(sx[n] + sy[n]);
+        }
+        s_H2[ig] = (T)go.H2;
+        s_WET[ig] = (T)go.WET;
+    }
+    __syncthreads();
+
+    // phase 1: dc/dq along direction d at Gauss point gp
+    if (t < 9 * EX_NDIR) {
+        const int gp = t / EX_NDIR, d = t - EX_NDIR * (t / EX_NDIR);
+        if (d < 20 || prm.nex > 0) {
+            typedef Dual<T> R;
+            TView<T> V{s_tl};
+            const Interp<T> Ip = interpolate(V, x_bfn[gp], s_dFx[gp], s_dFy[gp], s_d2x[gp],
+                                             s_d2y[gp]);
+            Interp<R> I;
+#define SEED(field, idx) I.field = R(Ip.field, d == (idx) ? (T)1 : (T)0)
+            SEED(U1, 0); SEED(GU11, 1); SEED(GU21, 2); SEED(lap1, 3);
+            SEED(U2, 4); SEED(GU12, 5); SEED(GU22, 6); SEED(lap2, 7);
+            SEED(P, 8); SEED(dPx, 9); SEED(dPy, 10);
+            SEED(S11, 11); SEED(dS11x, 12); SEED(dS11y, 13);
+            SEED(S12, 14); SEED(dS12x, 15); SEED(dS12y, 16);
+            SEED(S22, 17); SEED(dS22x, 18); SEED(dS22y, 19);
+#undef SEED
+            R WiN = R(prm.WiN);
+            if (prm.nex > 0) {
+                const T wi0 = (T)prm.Wi0;
+                WiN = R(wi0 * (T)a.EU[prm.nex - 1], d == 20 ? wi0 : (T)0);
+            }
+            R dotU[9];
+            const GpCoef<R> g =
+                gauss_point<FORM, SPEC>(I, prm, WiN, s_H2[gp], s_dFx[gp], s_dFy[gp], dotU);
+            T *dst = D + (gp * EX_NDIR + d) * 18;
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                R o[6];
+                const R du = k == 0 ? R(0.0) : (k == 1 ? g.U1 : g.U2);
+                test_node<FORM, SPEC>(g, prm, k == 0 ? 1.0 : 0.0, (T)(k == 1 ? 1 : 0),
+                                      (T)(k == 2 ? 1 : 0), du, (T)1, o);
+#pragma unroll
+                for (int q = 0; q < 6; q++) dst[q * 3 + k] = o[q].d;
+            }
+        }
+    }
+    __syncthreads();
+
+    // phase 2a: test-function side
+    for (int it = t; it < 9 * EX_NDIR * 9; it += EX_THREADS) {
+        const int i = it % 9;
+        const int gd = it / 9;               // gp*21 + d
+        const int gp = gd / EX_NDIR;
+        const T *dd = D + gd * 18;
+        const T b0 = (T)x_bfn[gp][i], b1 = s_dFx[gp][i], b2 = s_dFy[gp][i], w = s_WET[gp];
+        T *dst = A + gd * 54 + i * 6;
+#pragma unroll
+        for (int q = 0; q < 6; q++)
+            dst[q] = w * (b0 * dd[q * 3 + 0] + b1 * dd[q * 3 + 1] + b2 * dd[q * 3 + 2]);
+    }
+    __syncthreads();
+
+    // phase 2b: trial-function side, block layout ((i*9 + j)*36 + e*6 + f)
+    T *out = es + (size_t)e * 2916;
+    for (int o = t; o < 2916; o += EX_THREADS) {
+        const int ij = o / 36, r = o - 36 * (o / 36);
+        const int i = ij / 9, j = ij - 9 * (ij / 9);
+        const int q = r / 6, f = r - 6 * (r / 6);
+        const int ns = f < 2 ? 4 : 3;
+        T acc = 0;
+        for (int gp = 0; gp < 9; gp++) {
+            const T *ag = A + gp * EX_NDIR * 54 + i * 6 + q;
+            const int q0 = qdir(f, 0);
+            acc += ag[q0 * 54] * (T)x_bfn[gp][j];
+            acc += ag[(q0 + 1) * 54] * s_dFx[gp][j];
+            acc += ag[(q0 + 2) * 54] * s_dFy[gp][j];
+            if (ns == 4) acc += ag[(q0 + 3) * 54] * s_lap[gp][j];
+        }
+        out[o] = acc;
+    }
+    if (prm.nex > 0 && t < 54) {
+        T acc = 0;
+        for (int gp = 0; gp < 9; gp++) acc += A[(gp * EX_NDIR + 20) * 54 + t];
+        as[(size_t)e * 54 + t] = acc;
+    }
+}
+
+template <class T, int FORM>
+static cudaError_t launch_exact_form(const ElemArgs &a, const KParams &p, T *es, T *as,
+                                     cudaStream_t s)
+{
+    const int spec = (p.ReN == 0.0 ? SPEC_RE0 : 0) | (p.DfN == 0.0 ? SPEC_DF0 : 0);
+    const size_t smem = sizeof(T) * (9 * EX_NDIR * 18 + 9 * EX_NDIR * 54);
+    cudaError_t e = cudaSuccess;
+#define GO(SP)                                                                             \
+    e = cudaFuncSetAttribute(k_exact<T, FORM, SP>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                             (int)smem);                                                   \
+    if (e == cudaSuccess) k_exact<T, FORM, SP><<<a.nel, EX_THREADS, smem, s>>>(a, p, es, as);
+    switch (spec) {
+    case 0: GO(0) break;
+    case SPEC_RE0: GO(SPEC_RE0) break;
+    case SPEC_DF0: GO(SPEC_DF0) break;
+    default: GO(SPEC_RE0 | SPEC_DF0) break;
+    }
+#undef GO
+    if (e != cudaSuccess) return e;
+    return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_exact(const ElemArgs &a, const KParams &p, T *es, T *as, cudaStream_t s)
+{
+    if (a.nel <= 0) return cudaSuccess;
+    if (p.form == FORM_SQRT) return launch_exact_form<T, FORM_SQRT>(a, p, es, as, s);
+    return launch_exact_form<T, FORM_T>(a, p, es, as, s);
+}
+
+template cudaError_t launch_exact<float>(const ElemArgs &, const KParams &, float *, float *,
+                                         cudaStream_t);
+template cudaError_t launch_exact<double>(const ElemArgs &, const KParams &, double *, double *,
+                                          cudaStream_t);
+
+// FP32 scatter of the exact Jacobian (element order, as the FP64 one)
+__global__ void k_gather_jacobian32(const GatherArgs g, const float *__restrict__ es,
+                                    float *__restrict__ vals)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)g.nblocks * 36) return;
+    const int blk = (int)(t / 36);
+    const int r = (int)(t - (int64_t)blk * 36);
+    const int jeq = r / 6, ieq = r - 6 * (r / 6);
+    const int64_t slot = g.rowptr[(int64_t)g.brow[blk] * 6 + jeq] + g.boff[blk] + ieq;
+    float acc = vals[slot];
+    const int c0 = g.bptr[blk], c1 = g.bptr[blk + 1];
+    for (int c = c0; c < c1; c++) acc = acc + es[(int64_t)g.bcon[c] * 36 + r];
+    vals[slot] = acc;
+}
+
+__global__ void k_gather_arclength32(const GatherArgs g, const float *__restrict__ as,
+                                     float *__restrict__ vals)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)g.nnodes * 6) return;
+    const int node = (int)(t / 6), jeq = (int)(t - (int64_t)node * 6);
+    const int64_t slot = g.rowptr[t + 1] - 1;
+    float acc = vals[slot];
+    const int c0 = g.nptr[node], c1 = g.nptr[node + 1];
+    for (int c = c0; c < c1; c++) acc = acc + as[(int64_t)g.ncon[c] * 6 + jeq];
+    vals[slot] = acc;
+}
+
+cudaError_t launch_gather_jacobian32(const GatherArgs &g, const float *es, float *vals,
+                                     cudaStream_t s)
+{
+    const int64_t n = (int64_t)g.nblocks * 36;
+    if (n == 0) return cudaSuccess;
+    k_gather_jacobian32<<<(unsigned)((n + 287) / 288), 288, 0, s>>>(g, es, vals);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_arclength32(const GatherArgs &g, const float *as, float *vals,
+                                      cudaStream_t s)
+{
+    const int64_t n = (int64_t)g.nnodes * 6;
+    if (n == 0 || g.nex == 0) return cudaSuccess;
+    k_gather_arclength32<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(g, as, vals);
+    return cudaGetLastError();
+}
+
+}  // namespace vefem

@@ -76,6 +76,15 @@ cudaError_t launch_gather_jacobian(const GatherArgs &g, const double *es, double
 cudaError_t launch_gather_arclength(const GatherArgs &g, const double *as, double *vals,
                                     cudaStream_t s);
 
+// Exact-Jacobian kernels (vefem_exact.cu): element Jacobian and arclength column in T.
+cudaError_t upload_tables_exact(const GaussTables &t, cudaStream_t s);
+template <class T>
+cudaError_t launch_exact(const ElemArgs &a, const KParams &p, T *es, T *as, cudaStream_t s);
+cudaError_t launch_gather_jacobian32(const GatherArgs &g, const float *es, float *vals,
+                                     cudaStream_t s);
+cudaError_t launch_gather_arclength32(const GatherArgs &g, const float *as, float *vals,
+                                      cudaStream_t s);
+
 // Message returned by vefem_last_error(NULL) for entry points without a context.
 void set_global_error(const std::string &msg);
 

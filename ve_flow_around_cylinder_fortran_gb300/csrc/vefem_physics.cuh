@@ -31,6 +31,10 @@ enum { SPEC_RE0 = 1,   // ReN == 0: convection, LSME-momentum and (ReN/dt, ReN*t
        SPEC_DF0 = 2 }; // DfN == 0: stress diffusion terms and DfN/Helem^2
 enum { L_PTT = 0, M_L_PTT = 1, E_PTT = 2, M_E_PTT = 3, FENE_CR = 4, FENE_P = 5, GIESEKUS = 6 };
 
+// R is the scalar of state-dependent values, G the scalar of geometry values
+// (basis derivatives, weights); the FP64 kernels use R = G = double, the
+// exact-Jacobian kernels a dual number for R and float or double for G.
+
 // ---------------------------------------------------------------------------
 // Geometry of one Gauss point: basis2D (Element_Calculations_mod.F90:308-361),
 // Helem of setStabilizationTerms (:718-727) and WET (Equations_mod.F90:85).
@@ -194,9 +198,9 @@ VF_HD void interpolate_field(const View &V, int f, const double *bfn, const R *d
 // strongFormMomentum/Continuity (:658-697), setStabilizationTerms (:701-773).
 // dotU[n] = U . grad(phi_n) is returned for reuse by the test-function loop
 // (the reference computes the same product there).
-template <int FORM, int SPEC = 0, class R>
-VF_HD GpCoef<R> gauss_point(const Interp<R> &I, const KParams &prm, R WiN, R H2, const R *dFx,
-                            const R *dFy, R *dotU)
+template <int FORM, int SPEC = 0, class R, class G>
+VF_HD GpCoef<R> gauss_point(const Interp<R> &I, const KParams &prm, R WiN, G H2, const G *dFx,
+                            const G *dFy, R *dotU)
 {
     GpCoef<R> g;
     const double BvN = prm.BvN, ReN = prm.ReN, VeN = prm.VeN, DfN = prm.DfN;
@@ -449,9 +453,9 @@ VF_HD GpCoef<R> gauss_point(const Interp<R> &I, const KParams &prm, R WiN, R H2,
 
 // Weak-form terms of one test node n (momentumMain(SQRT), continuityBulkMain,
 // stressesBulkMain(SQRT), Residuals_mod.F90:44-157, 295-490) times WET.
-template <int FORM, int SPEC = 0, class R, class Out>
-VF_HD void test_node(const GpCoef<R> &g, const KParams &prm, double bifn, R fx, R fy, R du,
-                     R WET, Out *out)
+template <int FORM, int SPEC = 0, class R, class G, class Out>
+VF_HD void test_node(const GpCoef<R> &g, const KParams &prm, double bifn, G fx, G fy, R du,
+                     G WET, Out *out)
 {
     const R DfN = prm.DfN;
     // momentum

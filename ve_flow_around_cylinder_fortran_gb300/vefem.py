@@ -21,6 +21,9 @@ LIB_PATH = os.path.join(PKG, "_build", "libvefem.so")
 
 VEFEM_RESIDUAL = 0x1
 VEFEM_JAC_FD64 = 0x2
+VEFEM_JAC_EXACT64 = 0x4
+VEFEM_JAC_EXACT32 = 0x8
+JACOBIANS = {"fd64": VEFEM_JAC_FD64, "exact64": VEFEM_JAC_EXACT64, "exact32": VEFEM_JAC_EXACT32}
 VEFEM_ZERO_FIRST = 0x100
 VEFEM_OUTLET_EDGES = 0x200
 VEFEM_TIMING = 0x1000
@@ -164,8 +167,11 @@ class BulkAssembler:
                                            _ptr(vals), 1 if on_device else 0))
 
     def set_equations_bulk(self, TL, EU, flag_nr: str = "NRP", b=None, vals=None,
-                           zero_first: bool = False, outlet_edges: bool = False):
-        """setEquationsBulk on host arrays; returns (b, vals)."""
+                           zero_first: bool = False, outlet_edges: bool = False,
+                           jacobian: str = "fd64"):
+        """setEquationsBulk on host arrays; returns (b, vals).  ``jacobian``:
+        'fd64' (the reference's forward difference, bit-exact), 'exact64' or
+        'exact32' (exact derivative; float32 values for 'exact32')."""
         if flag_nr not in ("NRP", "MNR"):
             raise ValueError("flag_nr must be 'NRP' or 'MNR'")
         TL = np.ascontiguousarray(TL, dtype=np.float64)
@@ -174,9 +180,12 @@ class BulkAssembler:
             b = np.zeros(self.N)
         flags = VEFEM_RESIDUAL
         if flag_nr == "NRP":
-            flags |= VEFEM_JAC_FD64
+            flags |= JACOBIANS[jacobian]
+            dt = np.float32 if jacobian == "exact32" else np.float64
             if vals is None:
-                vals = np.zeros(self.nnz)
+                vals = np.zeros(self.nnz, dtype=dt)
+            elif vals.dtype != dt:
+                raise ValueError(f"vals must be {np.dtype(dt).name} for jacobian={jacobian}")
         else:
             vals = None
         if zero_first:
