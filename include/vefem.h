@@ -134,6 +134,18 @@ int vefem_set_params(vefem_ctx *ctx, const vefem_params *params);
 int vefem_assemble(vefem_ctx *ctx, const double *TL, const double *EU, int flags, double *b,
                    void *vals, int on_device);
 
+/* Dirichlet rows after assembly, as applyDirichletBC and
+ * applyDirichletBCFullyDeveloped do (Dirichlet_mod.F90:104-192):
+ * b[row] = TL(node, eq) - value (INSERT) for every listed row, and, when
+ * flags holds a Jacobian flag, the row's AIJ entries are zeroed and its
+ * diagonal set to 1 (MatZeroRows with diag = 1).  rows are 0-based global
+ * rows (node*6 + eq) of node unknowns, without duplicates; values the
+ * prescribed values.  flags: VEFEM_RESIDUAL (update b) and at most one
+ * Jacobian flag (VEFEM_JAC_EXACT32 means vals is float[nnz]).
+ * on_device = 1: rows, values, TL, b, vals are device pointers; 0: host. */
+int vefem_apply_dirichlet(vefem_ctx *ctx, int nrows, const int64_t *rows, const double *values,
+                          const double *TL, double *b, void *vals, int flags, int on_device);
+
 /* Per-kernel times (milliseconds, CUDA events on the context's stream) of the
  * last vefem_assemble called with VEFEM_TIMING:
  * t[0] element kernel, t[1] residual scatter, t[2] Jacobian scatter,

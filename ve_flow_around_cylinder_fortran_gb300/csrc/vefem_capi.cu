@@ -46,6 +46,9 @@ struct vefem_ctx {
     int32_t *d_brow = nullptr, *d_boff = nullptr, *d_bptr = nullptr, *d_bcon = nullptr;
     int32_t *d_edge_elem = nullptr, *d_edge_id = nullptr;
     int32_t *d_edge_row = nullptr, *d_edge_off = nullptr;   // [nedge][81]
+    int32_t *d_colind = nullptr;                            // for MatZeroRows on the device
+    std::vector<int64_t> h_rowptr;                          // host copies for host-side rows
+    std::vector<int32_t> h_colind;
     // device scratch / staging (allocated on first use)
     double *d_rs = nullptr, *d_es = nullptr, *d_as = nullptr;
     float *d_es32 = nullptr, *d_as32 = nullptr;
@@ -410,6 +413,8 @@ extern "C" int vefem_create(const vefem_mesh *mesh, const vefem_csr *pat,
     }
     ctx->nblocks = nblocks;
     ctx->nedge = nedge;
+    ctx->h_rowptr.assign(rowptr, rowptr + N + 1);
+    ctx->h_colind.assign(colind, colind + rowptr[N]);
 
     cudaError_t ce = cudaSetDevice(ctx->device);
     if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
@@ -434,6 +439,7 @@ extern "C" int vefem_create(const vefem_mesh *mesh, const vefem_csr *pat,
     UPL(d_conn, conn0.data(), conn0.size())
     UPL(d_xy, xy.data(), xy.size())
     UPL(d_rowptr, rowptr, (size_t)N + 1)
+    UPL(d_colind, colind, (size_t)rowptr[N])
     UPL(d_nptr, nptr.data(), nptr.size())
     UPL(d_ncon, ncon.data(), ncon.size())
     UPL(d_brow, brow.data(), brow.size())
@@ -672,6 +678,44 @@ extern "C" int vefem_assemble(vefem_ctx *ctx, const double *TL, const double *EU
     return VEFEM_OK;
 }
 
+extern "C" int vefem_apply_dirichlet(vefem_ctx *ctx, int nrows, const int64_t *rows,
+                                     const double *values, const double *TL, double *b,
+                                     void *vals, int flags, int on_device)
+{
+    if (!ctx) return VEFEM_ERR_ARG;
+    const int jmode = flags & (VEFEM_JAC_FD64 | VEFEM_JAC_EXACT64 | VEFEM_JAC_EXACT32);
+    if (jmode && (jmode & (jmode - 1))) return fail(ctx, VEFEM_ERR_ARG, "at most one Jacobian flag");
+    const bool want_res = flags & VEFEM_RESIDUAL;
+    if (nrows < 0 || (nrows > 0 && (!rows || !values))) return fail(ctx, VEFEM_ERR_ARG, "bad rows");
+    if (want_res && (!b || !TL)) return fail(ctx, VEFEM_ERR_ARG, "b or TL is NULL");
+    if (jmode && !vals) return fail(ctx, VEFEM_ERR_ARG, "vals is NULL");
+    const bool f32 = jmode == VEFEM_JAC_EXACT32;
+    const int64_t nd = (int64_t)ctx->nnodes * 6;
+    if (!on_device) {
+        for (int r = 0; r < nrows; r++)
+            if (rows[r] < 0 || rows[r] >= nd) return fail(ctx, VEFEM_ERR_ARG, "Dirichlet row out of range");
+        for (int r = 0; r < nrows; r++) {
+            const int64_t row = rows[r];
+            if (want_res) b[row] = TL[(row % 6) * ctx->nnodes + row / 6] - values[r];
+            if (jmode)
+                for (int64_t s = ctx->h_rowptr[row]; s < ctx->h_rowptr[row + 1]; s++) {
+                    const bool diag = ctx->h_colind[s] == row;
+                    if (f32)
+                        static_cast<float *>(vals)[s] = diag ? 1.0f : 0.0f;
+                    else
+                        static_cast<double *>(vals)[s] = diag ? 1.0 : 0.0;
+                }
+        }
+        return VEFEM_OK;
+    }
+    CK(cudaSetDevice(ctx->device));
+    CK(launch_dirichlet(nrows, ctx->nnodes, rows, values, TL, want_res ? b : nullptr,
+                        ctx->d_rowptr, ctx->d_colind, jmode ? vals : nullptr, f32 ? 1 : 0,
+                        ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return VEFEM_OK;
+}
+
 extern "C" int vefem_last_timing(const vefem_ctx *ctx, float *t, int n)
 {
     if (!ctx || !t) return VEFEM_ERR_ARG;
@@ -692,7 +736,7 @@ extern "C" int vefem_destroy(vefem_ctx *ctx)
                     ctx->d_boff, ctx->d_bptr, ctx->d_bcon, ctx->d_edge_elem, ctx->d_edge_id,
                     ctx->d_edge_row, ctx->d_edge_off, ctx->d_rs, ctx->d_es, ctx->d_as,
                     ctx->d_ers, ctx->d_ees, ctx->d_eas, ctx->d_TL, ctx->d_EU, ctx->d_b,
-                    ctx->d_vals, ctx->d_es32, ctx->d_as32, ctx->d_vals32};
+                    ctx->d_vals, ctx->d_es32, ctx->d_as32, ctx->d_vals32, ctx->d_colind};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int i = 0; i < 8; i++)

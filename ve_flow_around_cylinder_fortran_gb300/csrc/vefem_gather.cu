@@ -59,6 +59,42 @@ __global__ void k_gather_arclength(const GatherArgs g, const double *__restrict_
     vals[slot] = acc;
 }
 
+// Dirichlet rows: b = TL - value, and the AIJ row zeroed with 1 on the diagonal
+template <class V>
+__global__ void k_dirichlet(int nrows, int nnodes, const int64_t *__restrict__ rows,
+                            const double *__restrict__ values, const double *__restrict__ TL,
+                            double *b, const int64_t *__restrict__ rowptr,
+                            const int32_t *__restrict__ colind, V *vals)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrows) return;
+    const int64_t row = rows[r];
+    if (row < 0 || row >= (int64_t)nnodes * 6) return;   // rows outside the node unknowns are ignored
+    if (b) {
+        const int64_t node = row / 6, eq = row - 6 * (row / 6);
+        b[row] = TL[eq * nnodes + node] - values[r];
+    }
+    if (vals) {
+        for (int64_t s = rowptr[row]; s < rowptr[row + 1]; s++)
+            vals[s] = colind[s] == row ? (V)1 : (V)0;
+    }
+}
+
+cudaError_t launch_dirichlet(int nrows, int nnodes, const int64_t *rows, const double *values,
+                             const double *TL, double *b, const int64_t *rowptr,
+                             const int32_t *colind, void *vals, int vals_float, cudaStream_t s)
+{
+    if (nrows <= 0) return cudaSuccess;
+    const unsigned grid = (unsigned)((nrows + 127) / 128);
+    if (vals_float)
+        k_dirichlet<float><<<grid, 128, 0, s>>>(nrows, nnodes, rows, values, TL, b, rowptr, colind,
+                                                 static_cast<float *>(vals));
+    else
+        k_dirichlet<double><<<grid, 128, 0, s>>>(nrows, nnodes, rows, values, TL, b, rowptr,
+                                                  colind, static_cast<double *>(vals));
+    return cudaGetLastError();
+}
+
 static inline unsigned grid_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 cudaError_t launch_gather_residual(const GatherArgs &g, const double *rs, double *b,

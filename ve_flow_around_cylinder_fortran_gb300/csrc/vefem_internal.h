@@ -85,6 +85,10 @@ cudaError_t launch_gather_jacobian32(const GatherArgs &g, const float *es, float
 cudaError_t launch_gather_arclength32(const GatherArgs &g, const float *as, float *vals,
                                       cudaStream_t s);
 
+cudaError_t launch_dirichlet(int nrows, int nnodes, const int64_t *rows, const double *values,
+                             const double *TL, double *b, const int64_t *rowptr,
+                             const int32_t *colind, void *vals, int vals_float, cudaStream_t s);
+
 // Message returned by vefem_last_error(NULL) for entry points without a context.
 void set_global_error(const std::string &msg);
 

@@ -30,7 +30,8 @@ VEFEM_TIMING = 0x1000
 
 EXPORTED = ["vefem_abi_version", "vefem_create", "vefem_set_params", "vefem_assemble",
             "vefem_last_timing", "vefem_last_launch_count", "vefem_stream", "vefem_destroy",
-            "vefem_last_error", "vefem_build_pattern"]
+            "vefem_last_error", "vefem_build_pattern", "vefem_apply_dirichlet",
+            "vefem_algorithmic_ops", "vefem_assemble_residual_noalloc"]
 
 
 class VefemError(RuntimeError):
@@ -78,6 +79,7 @@ def load(path: str = LIB_PATH):
     L.vefem_last_error.argtypes = [P]
     L.vefem_last_error.restype = ctypes.c_char_p
     L.vefem_build_pattern.argtypes = [P, ctypes.c_int, P, P, P, P]
+    L.vefem_apply_dirichlet.argtypes = [P, ctypes.c_int, P, P, P, P, P, ctypes.c_int, ctypes.c_int]
     _lib = L
     return L
 
@@ -194,6 +196,18 @@ class BulkAssembler:
             flags |= VEFEM_OUTLET_EDGES
         self.assemble(TL, EU, flags, b, vals, on_device=False)
         return b, vals
+
+    def apply_dirichlet(self, rows, values, TL, b, vals, flags: int, on_device: bool = False,
+                        nrows: int | None = None):
+        """Dirichlet rows after assembly (applyDirichletBC): b = TL - value and,
+        with a Jacobian flag, MatZeroRows(diag = 1) on vals."""
+        n = int(nrows if nrows is not None else len(rows))
+        if not on_device:
+            rows = np.ascontiguousarray(rows, dtype=np.int64)
+            values = np.ascontiguousarray(values, dtype=np.float64)
+        self._check(self._L.vefem_apply_dirichlet(self._h, n, _ptr(rows), _ptr(values), _ptr(TL),
+                                                  _ptr(b), _ptr(vals), int(flags),
+                                                  1 if on_device else 0))
 
     def last_timing(self):
         t = (ctypes.c_float * 5)()
