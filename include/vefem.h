@@ -197,6 +197,36 @@ int vefem_assemble_residual_noalloc(const vefem_params *params, int nnodes, int 
 
 int vefem_abi_version(void);
 
+/* ---- Learned continuation predictor: network kernels ---------------------
+ * No counterpart in the reference (its arclength predictor is the tangent
+ * step of updateSolutionArclength, Continuation_Arclength_mod.F90:339-379).
+ * A multilayer perceptron in -> width -> ... -> width -> out with
+ * hidden_layers GELU layers (erf form) and a linear output, BF16 weights
+ * (FP32 master copies) with FP32 accumulation, trained by full-batch Adam
+ * (beta1 0.9, beta2 0.999, eps 1e-8) on the mean squared error.  Host
+ * pointers throughout; every call returns after its work has finished.
+ * Parameters are one FP32 array: for each layer W[out][in] then b[out]. */
+typedef struct vefem_mlp vefem_mlp;
+
+int vefem_mlp_create(int in_dim, int width, int out_dim, int hidden_layers, uint64_t seed,
+                     int device, vefem_mlp **out);
+int64_t vefem_mlp_num_params(const vefem_mlp *m);
+int vefem_mlp_set_params(vefem_mlp *m, const float *params, int64_t n);
+int vefem_mlp_get_params(const vefem_mlp *m, float *params, int64_t n);
+/* Y[n][out] = net(X[n][in]) */
+int vefem_mlp_forward(vefem_mlp *m, const float *X, int n, float *Y);
+/* loss = mean((net(X) - T)^2) and its gradient in the parameter layout */
+int vefem_mlp_loss_grad(vefem_mlp *m, const float *X, const float *T, int n, float *loss,
+                        float *grad);
+/* iters Adam iterations at learning rate lr (one CUDA graph per iteration);
+ * final_loss (may be NULL) receives the loss of the last iteration's forward */
+int vefem_mlp_train(vefem_mlp *m, const float *X, const float *T, int n, int iters, float lr,
+                    float *final_loss);
+/* Adam moments and step count back to zero (parameters kept) */
+int vefem_mlp_reset_optimizer(vefem_mlp *m);
+int vefem_mlp_destroy(vefem_mlp *m);
+const char *vefem_mlp_last_error(const vefem_mlp *m);
+
 #ifdef __cplusplus
 }
 #endif

@@ -13,6 +13,9 @@ class OracleAssembly:
         self.rows, self.values, self.edges = rows, values, edges
         self.nthreads = nthreads
 
+    def set_values(self, values):
+        self.values = values
+
     def __call__(self, TL, EU, want_jac):
         m = self.m
         b, v = O.assemble(self.p, m.conn, m.xyz, TL, EU, self.rp, self.ci, jacobian=want_jac,

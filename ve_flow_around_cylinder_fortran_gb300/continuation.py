@@ -1,0 +1,252 @@
+"""Pseudo-arclength continuation in the Weissenberg number over the GPU assembly.
+
+Restates the reference's arclength driver for the Cylinder_2D problem with
+Nex = 1 (the extra unknown lambda, Wi = Wi0 * lambda at every Gauss point):
+
+* continuationStepArclength (Continuation_Arclength_mod.F90:77-130): Newton
+  at the predicted point, then direction, step control and the next
+  prediction;
+* the lambda equation (arclength, Extra_Equations_mod.F90:698-768): for the
+  first two increments lambda is pinned, lambda - (LN0 + (k-1) dArN), with
+  the lambda row and column replaced by the unit vector (MatZeroRowsColumns);
+  afterwards pseudoArclength (:772-829): t . (x - x_o) - dS with the row
+  [dTLodS, dEUodS];
+* setDirectionVectors (:151-280): secant (x - x_o)/|x - x_o| at increment 2,
+  afterwards the tangent solving J t = e_lambda with the last factorised
+  Jacobian, normalised;
+* adjustContinuationStep (:282-337): err_pr = max over fields of
+  |x - x_p| / |x|, trns = sqrt(Eps_Pr / err_pr) capped at 2,
+  dS = min(dS trns, dS_max);
+* updateSolutionArclength (:339-379): the plain predictor x_p = x + t dS.
+
+A predictor object can replace the plain prediction (the learned POD/MLP
+predictor in ``learned.py``); Newton stays the corrector.  The host solves
+with SuperLU in a nested-dissection order (linsolve.py, stand-in for
+MUMPS); the dense lambda row and the arclength column make the matrix
+bordered, and the lambda unknown is ordered last.
+"""
+from __future__ import annotations
+
+import dataclasses
+import time
+
+import numpy as np
+
+from . import linsolve as LS
+from . import newton as NW
+from . import state as S
+
+EPS_PR = 1.0e-3
+DS_MAX = 50.0
+
+
+@dataclasses.dataclass
+class ArclengthSettings:
+    LN0: float = 1.0          # lambda of increment 1 (Wi = Wi0 * LN0)
+    dArN: float = 0.1         # lambda step of increment 2
+    dS0: float = 1.0          # first arclength step
+    dS_max: float = DS_MAX
+    eps_pr: float = EPS_PR
+    tol: float = 1.0e-10      # Newton tolerance on |s| and |R|
+    lam_max: float = 10.0     # stop once lambda >= lam_max
+    max_steps: int = 200
+
+
+@dataclasses.dataclass
+class StepRecord:
+    increment: int
+    wi: float
+    lam: float
+    dS: float
+    newton_iterations: int
+    factorisations: int
+    res_norm: float
+    predictor: str
+    pred_error: float
+    wall_s: float
+
+
+class LambdaRow:
+    """Host side of the lambda equation applied after assembly and Dirichlet."""
+
+    def __init__(self, rowptr: np.ndarray, colind: np.ndarray):
+        self.rowptr = rowptr
+        self.colind = colind
+        self.N = len(rowptr) - 1
+        self.last_col_slots = rowptr[1:-1] - 1          # last entry of every node row
+        assert np.all(colind[self.last_col_slots] == self.N - 1)
+        self.mode = "pinned"
+        self.target = 0.0
+        self.t = None          # direction (N,)
+        self.x_o = None        # previous converged point (N,)
+        self.dS = 0.0
+
+    def __call__(self, x: np.ndarray, b: np.ndarray, vals):
+        N = self.N
+        r0, r1 = self.rowptr[N - 1], self.rowptr[N]
+        if self.mode == "pinned":
+            b[N - 1] = x[N - 1] - self.target
+            if vals is not None:
+                vals[self.last_col_slots] = 0.0
+                vals[r0:r1] = 0.0
+                vals[r1 - 1] = 1.0
+        else:
+            b[N - 1] = float(np.dot(self.t, x - self.x_o)) - self.dS
+            if vals is not None:
+                vals[r0:r1] = self.t
+
+
+class ArclengthContinuation:
+    """loopArclength for one mesh and one assembler (nex = 1)."""
+
+    def __init__(self, asm, mesh, phys: S.Physics, jacobian: str = "fd64",
+                 settings: ArclengthSettings | None = None, outlet_edges: bool = True,
+                 log=None, assembly=None):
+        if phys.nex != 1:
+            raise ValueError("arclength continuation needs nex = 1")
+        self.asm, self.mesh, self.phys = asm, mesh, phys
+        self.cfg = settings or ArclengthSettings()
+        self.jacobian = jacobian
+        self.log = log
+        rows, values = NW.boundary_conditions(mesh, phys)
+        self.rows = rows
+        self.dev = assembly if assembly is not None else \
+            NW.DeviceAssembly(asm, rows, values, jacobian, outlet_edges)
+        self.lrow = LambdaRow(asm.rowptr, asm.colind)
+        self.solver = LS.SparseLU(asm.rowptr, asm.colind, mesh)
+        self.N = asm.N
+        self.nn = asm.nnodes
+
+    # state vector x = [TL in node-major order, lambda]
+    def pack(self, TL, EU):
+        return np.concatenate([TL.T.reshape(-1), EU])
+
+    def unpack(self, x):
+        return np.ascontiguousarray(x[:-1].reshape(self.nn, 6).T), x[-1:].copy()
+
+    def _update_inflow(self, lam: float):
+        # the inflow profile follows Wi = Wi0 * lambda (applyDirichletBCFullyDeveloped)
+        p = dataclasses.replace(self.phys, WiN=self.phys.Wi0 * lam)
+        rows, values = NW.boundary_conditions(self.mesh, p)
+        self.dev.set_values(values)
+
+    def _newton(self, x0: np.ndarray):
+        """Newton with the lambda row; returns (x, iterations, factorisations,
+        last residual norm, last LU or None)."""
+        cfg = self.cfg
+        x = x0.copy()
+        res_norm = cor_new = cor_old = 1.0
+        flag = "NRP"
+        lu = None
+        it = nfac = 0
+        while True:
+            if cor_new < cfg.tol and res_norm < cfg.tol:
+                return x, it, nfac, res_norm, lu, True
+            it += 1
+            if it % 10 == 0:
+                flag = "NRP"
+            TL, EU = self.unpack(x)
+            want = flag == "NRP" or lu is None
+            self._update_inflow(float(EU[0]))
+            b, vals = self.dev(TL, EU, want)
+            self.lrow(x, b, vals)
+            res_norm = float(np.linalg.norm(b))
+            if want:
+                lu = self.solver.factor(vals)
+                nfac += 1
+            s = lu.solve(b)
+            cor_new = float(np.linalg.norm(s))
+            if self.log:
+                self.log(f"   {it:3d}. {flag}: RES_NORM = {res_norm:.4e}, COR_NORM = {cor_new:.4e}")
+            if cor_new != cor_new or cor_new > NW.COR_NORM_DIV or it > NW.NITER:
+                return x, it, nfac, res_norm, lu, False
+            if flag == "NRP":
+                flag = "MNR" if cor_new < NW.MNR_EPS else "NRP"
+            else:
+                flag = "NRP" if cor_new > cor_old else "MNR"
+            cor_old = cor_new
+            x = x - s
+
+    def run(self, TL0: np.ndarray, EU0: np.ndarray, predictor=None):
+        """Continue from (TL0, EU0) until lambda >= lam_max; returns the step
+        records and the converged states."""
+        cfg = self.cfg
+        x_p = self.pack(TL0, EU0)
+        x_p[-1] = cfg.LN0
+        x_o = None
+        t = None
+        dS = cfg.dS0
+        records, states = [], []
+        for k in range(1, cfg.max_steps + 1):
+            t0 = time.perf_counter()
+            if k <= 2:
+                self.lrow.mode = "pinned"
+                self.lrow.target = cfg.LN0 + (k - 1) * cfg.dArN
+                x_p[-1] = self.lrow.target
+            else:
+                self.lrow.mode = "arclength"
+                self.lrow.t, self.lrow.x_o, self.lrow.dS = t, x_o, dS
+            pred_name = "plain"
+            if predictor is not None and k > 2:
+                cand = predictor.predict(k, x_o, t, dS, x_p)
+                if cand is not None:
+                    x_p, pred_name = self._judge(x_p, cand)
+            x, its, nfac, rn, lu, ok = self._newton(x_p)
+            if not ok:
+                raise RuntimeError(f"arclength Newton failed at increment {k}")
+            err_pr = 0.0
+            if k > 1:
+                TLc, EUc = self.unpack(x)
+                TLp, EUp = self.unpack(x_p)
+                e = [np.linalg.norm(TLc[f] - TLp[f]) / max(np.linalg.norm(TLc[f]), 1e-300)
+                     for f in range(6)]
+                e.append(abs(EUc[0] - EUp[0]) / max(abs(EUc[0]), 1e-300))
+                err_pr = max(e)
+            lam = float(x[-1])
+            wall = time.perf_counter() - t0
+            records.append(StepRecord(k, self.phys.Wi0 * lam, lam, dS, its, nfac, rn, pred_name,
+                                      err_pr, wall))
+            states.append(x.copy())
+            if self.log:
+                self.log(f"step {k}: Wi = {self.phys.Wi0 * lam:.4f}, Newton {its}, "
+                         f"pred {pred_name} err {err_pr:.2e}, dS = {dS:.3f}, {wall:.2f} s")
+            if predictor is not None:
+                predictor.observe(k, x, self.phys.Wi0 * lam)
+            if lam >= cfg.lam_max:
+                break
+            # direction (setDirectionVectors)
+            if k == 1:
+                t_new = None
+            elif k == 2:
+                d = x - x_o
+                t_new = d / np.linalg.norm(d)
+            else:
+                e_l = np.zeros(self.N)
+                e_l[-1] = 1.0
+                tv = lu.solve(e_l)
+                t_new = tv / np.linalg.norm(tv)
+                if np.dot(t_new, t) < 0.0:
+                    t_new = -t_new
+            # step size (adjustContinuationStep)
+            if k > 1:
+                trns = min(np.sqrt(cfg.eps_pr / max(err_pr, 1e-300)), 2.0)
+                dS = min(dS * trns, cfg.dS_max)
+            # prediction (updateSolutionArclength)
+            x_o = x.copy()
+            t = t_new
+            x_p = x.copy() if t is None else x + t * dS
+        return records, states
+
+    def _judge(self, x_plain, x_cand):
+        """Newton judges the learned prediction by residual norm: the candidate
+        is used only when its residual is smaller than the plain prediction's."""
+        r = []
+        for x in (x_plain, x_cand):
+            TL, EU = self.unpack(x)
+            self._update_inflow(float(EU[0]))
+            b, _ = self.dev(TL, EU, False)
+            self.lrow(x, b, None)
+            r.append(float(np.linalg.norm(b)))
+        if r[1] < r[0]:
+            return x_cand, "learned"
+        return x_plain, "plain"

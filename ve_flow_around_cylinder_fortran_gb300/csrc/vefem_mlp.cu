@@ -1,0 +1,501 @@
+// Small multilayer perceptron for the learned continuation predictor:
+// in -> width (GELU) -> ... -> width (GELU) -> out, trained online with Adam.
+//
+// Weights are kept as FP32 master copies and used in BF16 (rounded to
+// nearest even) in the forward and backward products, with FP32
+// accumulation; activations, gradients and the optimiser state are FP32.
+// GELU is the erf form, 0.5 x (1 + erf(x / sqrt 2)).  The loss is the mean
+// squared error over all outputs.  Batches are a few hundred rows at most, so
+// the products are plain tiled kernels on the CUDA cores; one training
+// iteration (forward, backward, Adam) is captured once in a CUDA graph and
+// replayed.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "vefem.h"
+#include "vefem_internal.h"
+
+namespace {
+
+constexpr int TILE = 16;
+
+struct Layer {
+    int in, out;
+    float *W = nullptr, *b = nullptr;          // FP32 master [out][in], [out]
+    __nv_bfloat16 *Wb = nullptr;               // BF16 copy used by the products
+    float *mW = nullptr, *vW = nullptr, *mb = nullptr, *vb = nullptr;   // Adam moments
+    float *gW = nullptr, *gb = nullptr;        // gradients
+    float *Z = nullptr, *A = nullptr;          // pre-activation, activation [n][out]
+    float *dA = nullptr;                       // gradient w.r.t. A [n][out]
+};
+
+// Y[n][out] = X[n][in] . W^T + b, optional GELU; Z keeps the pre-activation
+__global__ void k_linear_fwd(const float *__restrict__ X, int n, int in,
+                             const __nv_bfloat16 *__restrict__ W, const float *__restrict__ b,
+                             int out, float *__restrict__ Z, float *__restrict__ A, int gelu)
+{
+    __shared__ float sx[TILE][TILE + 1], sw[TILE][TILE + 1];
+    const int r = blockIdx.y * TILE + threadIdx.y;     // sample
+    const int c = blockIdx.x * TILE + threadIdx.x;     // output unit
+    float acc = 0.0f;
+    for (int k0 = 0; k0 < in; k0 += TILE) {
+        const int kx = k0 + threadIdx.x, kw = k0 + threadIdx.y;
+        sx[threadIdx.y][threadIdx.x] = (r < n && kx < in) ? X[(size_t)r * in + kx] : 0.0f;
+        const int wc = blockIdx.x * TILE + threadIdx.x;
+        sw[threadIdx.y][threadIdx.x] =
+            (wc < out && kw < in) ? __bfloat162float(W[(size_t)wc * in + kw]) : 0.0f;
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < TILE; k++) acc += sx[threadIdx.y][k] * sw[k][threadIdx.x];
+        __syncthreads();
+    }
+    if (r < n && c < out) {
+        const float z = acc + b[c];
+        Z[(size_t)r * out + c] = z;
+        A[(size_t)r * out + c] = gelu ? 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)) : z;
+    }
+}
+
+// dZ = dA * gelu'(Z) (in place into dA when gelu)
+__global__ void k_gelu_bwd(int count, const float *__restrict__ Z, float *__restrict__ dA)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const float z = Z[i];
+    const float cdf = 0.5f * (1.0f + erff(z * 0.70710678118654752f));
+    const float pdf = 0.39894228040143268f * expf(-0.5f * z * z);
+    dA[i] = dA[i] * (cdf + z * pdf);
+}
+
+// dX[n][in] = dZ[n][out] . W[out][in]
+__global__ void k_linear_bwd_x(const float *__restrict__ dZ, int n, int out,
+                               const __nv_bfloat16 *__restrict__ W, int in,
+                               float *__restrict__ dX)
+{
+    __shared__ float sd[TILE][TILE + 1], sw[TILE][TILE + 1];
+    const int r = blockIdx.y * TILE + threadIdx.y;
+    const int c = blockIdx.x * TILE + threadIdx.x;     // input unit
+    float acc = 0.0f;
+    for (int k0 = 0; k0 < out; k0 += TILE) {
+        const int kd = k0 + threadIdx.x, kw = k0 + threadIdx.y;
+        sd[threadIdx.y][threadIdx.x] = (r < n && kd < out) ? dZ[(size_t)r * out + kd] : 0.0f;
+        sw[threadIdx.y][threadIdx.x] =
+            (c < in && kw < out) ? __bfloat162float(W[(size_t)kw * in + c]) : 0.0f;
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < TILE; k++) acc += sd[threadIdx.y][k] * sw[k][threadIdx.x];
+        __syncthreads();
+    }
+    if (r < n && c < in) dX[(size_t)r * in + c] = acc;
+}
+
+// gW[out][in] = dZ^T . X, gb[out] = sum over samples of dZ
+__global__ void k_linear_bwd_w(const float *__restrict__ dZ, const float *__restrict__ X, int n,
+                               int out, int in, float *__restrict__ gW, float *__restrict__ gb)
+{
+    __shared__ float sd[TILE][TILE + 1], sx[TILE][TILE + 1];
+    const int o = blockIdx.y * TILE + threadIdx.y;
+    const int c = blockIdx.x * TILE + threadIdx.x;
+    float acc = 0.0f, accb = 0.0f;
+    for (int k0 = 0; k0 < n; k0 += TILE) {
+        const int kd = k0 + threadIdx.x, kx = k0 + threadIdx.y;
+        sd[threadIdx.y][threadIdx.x] = (o < out && kd < n) ? dZ[(size_t)kd * out + o] : 0.0f;
+        sx[threadIdx.y][threadIdx.x] = (c < in && kx < n) ? X[(size_t)kx * in + c] : 0.0f;
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < TILE; k++) {
+            acc += sd[threadIdx.y][k] * sx[k][threadIdx.x];
+            accb += sd[threadIdx.y][k];
+        }
+        __syncthreads();
+    }
+    if (o < out && c < in) gW[(size_t)o * in + c] = acc;
+    if (o < out && blockIdx.x == 0 && threadIdx.x == 0) gb[o] = accb;
+}
+
+// MSE loss and its gradient: dY = 2 (Y - T) / (n out); loss accumulated in *loss
+__global__ void k_mse(int count, const float *__restrict__ Y, const float *__restrict__ T,
+                      float *__restrict__ dY, float *__restrict__ loss)
+{
+    __shared__ float red[256];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float d = 0.0f;
+    if (i < count) {
+        d = Y[i] - T[i];
+        dY[i] = 2.0f * d / (float)count;
+    }
+    red[threadIdx.x] = d * d;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) atomicAdd(loss, red[0] / (float)count);
+}
+
+// Adam on the FP32 masters, then the BF16 copy; t is read from device memory
+__global__ void k_adam(int count, float *__restrict__ p, const float *__restrict__ g,
+                       float *__restrict__ m, float *__restrict__ v, __nv_bfloat16 *pb, float lr,
+                       const int *__restrict__ step)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    const float t = (float)(*step);
+    const float mi = b1 * m[i] + (1.0f - b1) * g[i];
+    const float vi = b2 * v[i] + (1.0f - b2) * g[i] * g[i];
+    m[i] = mi;
+    v[i] = vi;
+    const float mh = mi / (1.0f - powf(b1, t));
+    const float vh = vi / (1.0f - powf(b2, t));
+    const float np = p[i] - lr * mh / (sqrtf(vh) + eps);
+    p[i] = np;
+    if (pb) pb[i] = __float2bfloat16_rn(np);
+}
+
+__global__ void k_to_bf16(int count, const float *__restrict__ p, __nv_bfloat16 *pb)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) pb[i] = __float2bfloat16_rn(p[i]);
+}
+
+__global__ void k_step_inc(int *step, float *loss)
+{
+    *step += 1;
+    *loss = 0.0f;
+}
+
+}  // namespace
+
+
+struct vefem_mlp {
+    int device = 0;
+    int in = 0, width = 0, out = 0, hidden = 0;
+    std::vector<Layer> L;
+    int cap = 0;                  // rows the activation buffers hold
+    float *X = nullptr, *T = nullptr, *loss = nullptr;
+    int *step = nullptr;
+    cudaStream_t s = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    int graph_n = -1;
+    float graph_lr = 0.0f;
+    std::string err;
+};
+
+namespace {
+
+int mlp_fail(vefem_mlp *m, int code, const std::string &msg)
+{
+    if (m)
+        m->err = msg;
+    else
+        vefem::set_global_error(msg);
+    return code;
+}
+
+#define MCK(call)                                                                   \
+    do {                                                                            \
+        cudaError_t _e = (call);                                                    \
+        if (_e != cudaSuccess)                                                      \
+            return mlp_fail(m, VEFEM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e)); \
+    } while (0)
+
+int64_t nparams(const vefem_mlp *m)
+{
+    int64_t n = 0;
+    for (const Layer &l : m->L) n += (int64_t)l.in * l.out + l.out;
+    return n;
+}
+
+int ensure_rows(vefem_mlp *m, int n)
+{
+    if (n <= m->cap) return VEFEM_OK;
+    for (Layer &l : m->L) {
+        cudaFree(l.Z);
+        cudaFree(l.A);
+        cudaFree(l.dA);
+        MCK(cudaMalloc(&l.Z, sizeof(float) * n * l.out));
+        MCK(cudaMalloc(&l.A, sizeof(float) * n * l.out));
+        MCK(cudaMalloc(&l.dA, sizeof(float) * n * l.out));
+    }
+    cudaFree(m->X);
+    cudaFree(m->T);
+    MCK(cudaMalloc(&m->X, sizeof(float) * n * m->in));
+    MCK(cudaMalloc(&m->T, sizeof(float) * n * m->out));
+    m->cap = n;
+    if (m->graph) {
+        cudaGraphExecDestroy(m->graph);
+        m->graph = nullptr;
+    }
+    return VEFEM_OK;
+}
+
+void launch_forward(vefem_mlp *m, int n)
+{
+    const float *x = m->X;
+    for (size_t i = 0; i < m->L.size(); i++) {
+        Layer &l = m->L[i];
+        dim3 bs(TILE, TILE), gs((l.out + TILE - 1) / TILE, (n + TILE - 1) / TILE);
+        k_linear_fwd<<<gs, bs, 0, m->s>>>(x, n, l.in, l.Wb, l.b, l.out, l.Z, l.A,
+                                          i + 1 < m->L.size() ? 1 : 0);
+        x = l.A;
+    }
+}
+
+void launch_backward(vefem_mlp *m, int n)
+{
+    // dA of the output layer holds dLoss/dY (from k_mse)
+    for (int i = (int)m->L.size() - 1; i >= 0; i--) {
+        Layer &l = m->L[i];
+        if (i + 1 < (int)m->L.size())
+            k_gelu_bwd<<<(n * l.out + 255) / 256, 256, 0, m->s>>>(n * l.out, l.Z, l.dA);
+        const float *xin = i == 0 ? m->X : m->L[i - 1].A;
+        dim3 bs(TILE, TILE), gw((l.in + TILE - 1) / TILE, (l.out + TILE - 1) / TILE);
+        k_linear_bwd_w<<<gw, bs, 0, m->s>>>(l.dA, xin, n, l.out, l.in, l.gW, l.gb);
+        if (i > 0) {
+            dim3 gx((l.in + TILE - 1) / TILE, (n + TILE - 1) / TILE);
+            k_linear_bwd_x<<<gx, bs, 0, m->s>>>(l.dA, n, l.out, l.Wb, l.in, m->L[i - 1].dA);
+        }
+    }
+}
+
+void launch_loss(vefem_mlp *m, int n)
+{
+    Layer &o = m->L.back();
+    const int count = n * o.out;
+    k_mse<<<(count + 255) / 256, 256, 0, m->s>>>(count, o.A, m->T, o.dA, m->loss);
+}
+
+void launch_adam(vefem_mlp *m, float lr)
+{
+    for (Layer &l : m->L) {
+        const int cw = l.in * l.out;
+        k_adam<<<(cw + 255) / 256, 256, 0, m->s>>>(cw, l.W, l.gW, l.mW, l.vW, l.Wb, lr, m->step);
+        k_adam<<<(l.out + 255) / 256, 256, 0, m->s>>>(l.out, l.b, l.gb, l.mb, l.vb, nullptr, lr,
+                                                       m->step);
+    }
+}
+
+}  // namespace
+
+namespace {
+
+int mlp_init(vefem_mlp *m, uint64_t seed)
+{
+    const int hidden_layers = m->hidden;
+    MCK(cudaSetDevice(m->device));
+    MCK(cudaStreamCreateWithFlags(&m->s, cudaStreamNonBlocking));
+    // Kaiming-uniform-like init from a 64-bit LCG (deterministic for a seed)
+    uint64_t st = seed * 6364136223846793005ULL + 1442695040888963407ULL;
+    auto uni = [&st]() {
+        st = st * 6364136223846793005ULL + 1442695040888963407ULL;
+        return (double)(st >> 11) * (1.0 / 9007199254740992.0);
+    };
+    for (int i = 0; i <= hidden_layers; i++) {
+        Layer l;
+        l.in = i == 0 ? m->in : m->width;
+        l.out = i == hidden_layers ? m->out : m->width;
+        m->L.push_back(l);
+    }
+    for (Layer &l : m->L) {
+        const size_t nw = (size_t)l.in * l.out;
+        std::vector<float> w(nw), b(l.out, 0.0f);
+        const double bound = std::sqrt(1.0 / l.in);
+        for (size_t k = 0; k < nw; k++) w[k] = (float)((2.0 * uni() - 1.0) * bound);
+        float **f[] = {&l.W, &l.mW, &l.vW, &l.gW};
+        for (float **p : f) MCK(cudaMalloc(p, sizeof(float) * nw));
+        float **g[] = {&l.b, &l.mb, &l.vb, &l.gb};
+        for (float **p : g) MCK(cudaMalloc(p, sizeof(float) * l.out));
+        MCK(cudaMalloc(&l.Wb, sizeof(__nv_bfloat16) * nw));
+        MCK(cudaMemcpy(l.W, w.data(), sizeof(float) * nw, cudaMemcpyHostToDevice));
+        MCK(cudaMemcpy(l.b, b.data(), sizeof(float) * l.out, cudaMemcpyHostToDevice));
+        MCK(cudaMemset(l.mW, 0, sizeof(float) * nw));
+        MCK(cudaMemset(l.vW, 0, sizeof(float) * nw));
+        MCK(cudaMemset(l.mb, 0, sizeof(float) * l.out));
+        MCK(cudaMemset(l.vb, 0, sizeof(float) * l.out));
+        k_to_bf16<<<(int)((nw + 255) / 256), 256, 0, m->s>>>((int)nw, l.W, l.Wb);
+    }
+    MCK(cudaMalloc(&m->loss, sizeof(float)));
+    MCK(cudaMalloc(&m->step, sizeof(int)));
+    MCK(cudaMemset(m->step, 0, sizeof(int)));
+    MCK(cudaStreamSynchronize(m->s));
+    return VEFEM_OK;
+}
+
+}  // namespace
+
+extern "C" int vefem_mlp_create(int in_dim, int width, int out_dim, int hidden_layers,
+                                uint64_t seed, int device, vefem_mlp **out)
+{
+    if (!out || in_dim <= 0 || width <= 0 || out_dim <= 0 || hidden_layers <= 0 || device < 0 ||
+        (int64_t)in_dim * width > (1 << 28) || (int64_t)width * out_dim > (1 << 28))
+        return mlp_fail(nullptr, VEFEM_ERR_ARG, "vefem_mlp_create: bad arguments");
+    *out = nullptr;
+    vefem_mlp *m = new vefem_mlp();
+    m->device = device;
+    m->in = in_dim;
+    m->width = width;
+    m->out = out_dim;
+    m->hidden = hidden_layers;
+    if (int rc = mlp_init(m, seed)) {
+        vefem::set_global_error("vefem_mlp_create: " + m->err);
+        vefem_mlp_destroy(m);
+        return rc;
+    }
+    *out = m;
+    return VEFEM_OK;
+}
+
+extern "C" int vefem_mlp_reset_optimizer(vefem_mlp *m)
+{
+    if (!m) return mlp_fail(nullptr, VEFEM_ERR_ARG, "NULL network");
+    MCK(cudaSetDevice(m->device));
+    for (Layer &l : m->L) {
+        const size_t nw = (size_t)l.in * l.out;
+        MCK(cudaMemsetAsync(l.mW, 0, sizeof(float) * nw, m->s));
+        MCK(cudaMemsetAsync(l.vW, 0, sizeof(float) * nw, m->s));
+        MCK(cudaMemsetAsync(l.mb, 0, sizeof(float) * l.out, m->s));
+        MCK(cudaMemsetAsync(l.vb, 0, sizeof(float) * l.out, m->s));
+    }
+    MCK(cudaMemsetAsync(m->step, 0, sizeof(int), m->s));
+    MCK(cudaStreamSynchronize(m->s));
+    return VEFEM_OK;
+}
+
+extern "C" int64_t vefem_mlp_num_params(const vefem_mlp *m) { return m ? nparams(m) : -1; }
+
+// parameters as one FP32 array: for each layer W [out][in] then b [out]
+extern "C" int vefem_mlp_set_params(vefem_mlp *m, const float *p, int64_t n)
+{
+    if (!m || !p || n != nparams(m)) return mlp_fail(m, VEFEM_ERR_ARG, "parameter count");
+    MCK(cudaSetDevice(m->device));
+    int64_t o = 0;
+    for (Layer &l : m->L) {
+        const size_t nw = (size_t)l.in * l.out;
+        MCK(cudaMemcpyAsync(l.W, p + o, sizeof(float) * nw, cudaMemcpyHostToDevice, m->s));
+        o += nw;
+        MCK(cudaMemcpyAsync(l.b, p + o, sizeof(float) * l.out, cudaMemcpyHostToDevice, m->s));
+        o += l.out;
+        k_to_bf16<<<(int)((nw + 255) / 256), 256, 0, m->s>>>((int)nw, l.W, l.Wb);
+    }
+    MCK(cudaStreamSynchronize(m->s));
+    return VEFEM_OK;
+}
+
+extern "C" int vefem_mlp_get_params(const vefem_mlp *mc, float *p, int64_t n)
+{
+    vefem_mlp *m = const_cast<vefem_mlp *>(mc);
+    if (!m || !p || n != nparams(m)) return mlp_fail(m, VEFEM_ERR_ARG, "parameter count");
+    MCK(cudaSetDevice(m->device));
+    int64_t o = 0;
+    for (Layer &l : m->L) {
+        const size_t nw = (size_t)l.in * l.out;
+        MCK(cudaMemcpyAsync(p + o, l.W, sizeof(float) * nw, cudaMemcpyDeviceToHost, m->s));
+        o += nw;
+        MCK(cudaMemcpyAsync(p + o, l.b, sizeof(float) * l.out, cudaMemcpyDeviceToHost, m->s));
+        o += l.out;
+    }
+    MCK(cudaStreamSynchronize(m->s));
+    return VEFEM_OK;
+}
+
+extern "C" int vefem_mlp_forward(vefem_mlp *m, const float *X, int n, float *Y)
+{
+    if (!m || !X || !Y || n <= 0) return mlp_fail(m, VEFEM_ERR_ARG, "bad arguments");
+    MCK(cudaSetDevice(m->device));
+    if (int rc = ensure_rows(m, n)) return rc;
+    MCK(cudaMemcpyAsync(m->X, X, sizeof(float) * n * m->in, cudaMemcpyHostToDevice, m->s));
+    launch_forward(m, n);
+    MCK(cudaGetLastError());
+    MCK(cudaMemcpyAsync(Y, m->L.back().A, sizeof(float) * n * m->out, cudaMemcpyDeviceToHost, m->s));
+    MCK(cudaStreamSynchronize(m->s));
+    return VEFEM_OK;
+}
+
+// loss and the gradient w.r.t. all parameters (layout of vefem_mlp_get_params)
+extern "C" int vefem_mlp_loss_grad(vefem_mlp *m, const float *X, const float *T, int n,
+                                   float *loss, float *grad)
+{
+    if (!m || !X || !T || !loss || !grad || n <= 0) return mlp_fail(m, VEFEM_ERR_ARG, "bad arguments");
+    MCK(cudaSetDevice(m->device));
+    if (int rc = ensure_rows(m, n)) return rc;
+    MCK(cudaMemcpyAsync(m->X, X, sizeof(float) * n * m->in, cudaMemcpyHostToDevice, m->s));
+    MCK(cudaMemcpyAsync(m->T, T, sizeof(float) * n * m->out, cudaMemcpyHostToDevice, m->s));
+    MCK(cudaMemsetAsync(m->loss, 0, sizeof(float), m->s));
+    launch_forward(m, n);
+    launch_loss(m, n);
+    launch_backward(m, n);
+    MCK(cudaGetLastError());
+    int64_t o = 0;
+    for (Layer &l : m->L) {
+        const size_t nw = (size_t)l.in * l.out;
+        MCK(cudaMemcpyAsync(grad + o, l.gW, sizeof(float) * nw, cudaMemcpyDeviceToHost, m->s));
+        o += nw;
+        MCK(cudaMemcpyAsync(grad + o, l.gb, sizeof(float) * l.out, cudaMemcpyDeviceToHost, m->s));
+        o += l.out;
+    }
+    MCK(cudaMemcpyAsync(loss, m->loss, sizeof(float), cudaMemcpyDeviceToHost, m->s));
+    MCK(cudaStreamSynchronize(m->s));
+    return VEFEM_OK;
+}
+
+// iters full-batch Adam iterations on (X, T); one iteration is a CUDA graph
+extern "C" int vefem_mlp_train(vefem_mlp *m, const float *X, const float *T, int n, int iters,
+                               float lr, float *final_loss)
+{
+    if (!m || !X || !T || n <= 0 || iters < 0) return mlp_fail(m, VEFEM_ERR_ARG, "bad arguments");
+    MCK(cudaSetDevice(m->device));
+    if (int rc = ensure_rows(m, n)) return rc;
+    MCK(cudaMemcpyAsync(m->X, X, sizeof(float) * n * m->in, cudaMemcpyHostToDevice, m->s));
+    MCK(cudaMemcpyAsync(m->T, T, sizeof(float) * n * m->out, cudaMemcpyHostToDevice, m->s));
+    if (!m->graph || m->graph_n != n || m->graph_lr != lr) {
+        if (m->graph) cudaGraphExecDestroy(m->graph);
+        m->graph = nullptr;
+        cudaGraph_t g;
+        MCK(cudaStreamBeginCapture(m->s, cudaStreamCaptureModeThreadLocal));
+        k_step_inc<<<1, 1, 0, m->s>>>(m->step, m->loss);
+        launch_forward(m, n);
+        launch_loss(m, n);
+        launch_backward(m, n);
+        launch_adam(m, lr);
+        MCK(cudaStreamEndCapture(m->s, &g));
+        MCK(cudaGraphInstantiate(&m->graph, g, 0));
+        cudaGraphDestroy(g);
+        m->graph_n = n;
+        m->graph_lr = lr;
+    }
+    for (int i = 0; i < iters; i++) MCK(cudaGraphLaunch(m->graph, m->s));
+    if (final_loss) {
+        MCK(cudaMemcpyAsync(final_loss, m->loss, sizeof(float), cudaMemcpyDeviceToHost, m->s));
+    }
+    MCK(cudaStreamSynchronize(m->s));
+    return VEFEM_OK;
+}
+
+extern "C" int vefem_mlp_destroy(vefem_mlp *m)
+{
+    if (!m) return VEFEM_OK;
+    cudaSetDevice(m->device);
+    if (m->s) cudaStreamSynchronize(m->s);
+    if (m->graph) cudaGraphExecDestroy(m->graph);
+    for (Layer &l : m->L) {
+        void *p[] = {l.W, l.b, l.Wb, l.mW, l.vW, l.mb, l.vb, l.gW, l.gb, l.Z, l.A, l.dA};
+        for (void *q : p)
+            if (q) cudaFree(q);
+    }
+    void *p[] = {m->X, m->T, m->loss, m->step};
+    for (void *q : p)
+        if (q) cudaFree(q);
+    if (m->s) cudaStreamDestroy(m->s);
+    delete m;
+    return VEFEM_OK;
+}
+
+extern "C" const char *vefem_mlp_last_error(const vefem_mlp *m) { return m ? m->err.c_str() : ""; }

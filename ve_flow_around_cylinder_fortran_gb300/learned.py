@@ -1,0 +1,153 @@
+"""Learned predictor for the arclength continuation.
+
+The reference predicts the next continuation point with the tangent step
+x_p = x + t dS (updateSolutionArclength, Continuation_Arclength_mod.F90:339-379).
+This module adds a learned prediction in a reduced space:
+
+* POD: the converged snapshots x_1..x_m (state vector [TL, lambda]) are
+  centred on their mean and decomposed by the method of snapshots (Gram
+  matrix on the GPU, its eigenvectors on the host, modes re-orthonormalised
+  by QR); up to ``n_modes`` modes Phi with coefficients
+  a_j = Phi^T (x_j - mean).
+* Network: the library's multilayer perceptron (vefem.MLP: 3 GELU layers of
+  width 256, BF16 weights, FP32 accumulation, trained by the library's own
+  forward, backward and Adam kernels).  Input of the sample for point j:
+  Wi_{j-1}, the arclength step ds_j = s_j - s_{j-1}, the last coefficient
+  vector a_{j-1} and the two last slopes (a_{j-1} - a_{j-2}) / ds_{j-1},
+  (a_{j-2} - a_{j-3}) / ds_{j-2} (the last three coefficient vectors in
+  difference form).  Output: the change of slope
+  (a_j - a_{j-1}) / ds_j - (a_{j-1} - a_{j-2}) / ds_{j-1}; an output of zero is
+  the secant predictor in the reduced space.  Inputs and outputs are
+  standardised over the training set.
+* Online training: once ``start`` points have converged, the basis is
+  rebuilt and the network retrained (warm start) on all samples after every
+  converged point.
+* Prediction: a = a_m + dS (quad + net(...)) with quad the quadratic
+  extrapolation of the slopes, and the candidate x = mean + Phi a.  The
+  candidate does not use the tangent: the tangent is solved with the last
+  factorised Jacobian, taken at the first Newton iterate rather than at the
+  converged point, and most of the tangent step's error lies outside the
+  span of the converged snapshots.
+
+Newton stays the corrector and the judge: the continuation takes the
+candidate only when its residual norm is below the tangent prediction's
+(ArclengthContinuation._judge).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+class LearnedPredictor:
+    def __init__(self, n_modes: int = 32, start: int = 20, width: int = 256, hidden: int = 3,
+                 iters: int = 400, lr: float = 1.0e-3, seed: int = 0, device: str = "cuda:0",
+                 net=None, log=None):
+        import torch
+        self.torch = torch
+        self.dev = torch.device(device)
+        self.n_modes, self.start = n_modes, start
+        self.iters, self.lr = iters, lr
+        self.in_dim = 2 + 3 * n_modes
+        if net is None:
+            from . import vefem as V
+            net = V.MLP(self.in_dim, n_modes, width=width, hidden=hidden, seed=seed,
+                        device=self.dev.index or 0)
+        self.net = net
+        self.log = log
+        self.X = []          # snapshots (device tensors)
+        self.wi = []
+        self.s = [0.0]       # cumulative chord length at each snapshot
+        self.basis = None    # (mean, Phi)
+        self.norm = None     # (xm, xs, ym, ys)
+        self.coef = None     # [m][r] coefficients of the snapshots
+        self.last_loss = None
+        self.trainings = 0
+
+    # ---- data --------------------------------------------------------------
+    def observe(self, k: int, x: np.ndarray, wi: float):
+        t = self.torch.from_numpy(np.ascontiguousarray(x, dtype=np.float64)).to(self.dev)
+        if self.X:
+            self.s.append(self.s[-1] + float(self.torch.linalg.vector_norm(t - self.X[-1])))
+        self.X.append(t)
+        self.wi.append(float(wi))
+        if len(self.X) >= self.start:
+            self._fit()
+
+    def _pod(self):
+        torch = self.torch
+        Xm = torch.stack(self.X, dim=1)                       # N x m
+        mean = Xm.mean(dim=1)
+        Xc = Xm - mean[:, None]
+        G = (Xc.T @ Xc).cpu().numpy()
+        lam, V = np.linalg.eigh(G)
+        order = np.argsort(lam)[::-1]
+        lam, V = lam[order], V[:, order]
+        keep = lam > lam[0] * 1e-14          # drop round-off directions
+        r = min(self.n_modes, int(keep.sum()))
+        lam, V = lam[:r], V[:, :r]
+        W = torch.from_numpy(V / np.sqrt(lam)).to(self.dev)
+        # re-orthonormalised: the snapshot method loses orthogonality in the
+        # weak modes by round-off ~ eps * lam_0 / lam_i
+        Phi = torch.linalg.qr(Xc @ W)[0]                      # N x r
+        if self.basis is not None:                            # keep mode signs stable
+            old = self.basis[1]
+            rr = min(r, old.shape[1])
+            sgn = torch.sign((Phi[:, :rr] * old[:, :rr]).sum(dim=0))
+            sgn[sgn == 0] = 1.0
+            Phi[:, :rr] *= sgn
+        coef = (Phi.T @ Xc).T.cpu().numpy()                   # m x r
+        if r < self.n_modes:
+            coef = np.pad(coef, ((0, 0), (0, self.n_modes - r)))
+        return mean, Phi, coef
+
+    def _features(self, j: int, ds_j: float, coef: np.ndarray):
+        """Network input of the sample for point j (0-based, j >= 3) and the
+        quadratic-extrapolation slope of the step s_{j-1} -> s_j."""
+        ds1 = self.s[j - 1] - self.s[j - 2]
+        ds2 = self.s[j - 2] - self.s[j - 3]
+        sl1 = (coef[j - 1] - coef[j - 2]) / ds1
+        sl2 = (coef[j - 2] - coef[j - 3]) / ds2
+        # slopes are derivatives at interval midpoints: exact for a quadratic a(s)
+        quad = sl1 + (sl1 - sl2) * (ds_j + ds1) / (ds1 + ds2)
+        return np.concatenate([[self.wi[j - 1], ds_j], coef[j - 1], sl1, sl2]), quad
+
+    def _dataset(self, coef):
+        X, Y = [], []
+        for j in range(3, len(self.X)):
+            ds = self.s[j] - self.s[j - 1]
+            f, quad = self._features(j, ds, coef)
+            X.append(f)
+            Y.append((coef[j] - coef[j - 1]) / ds - quad)
+        return np.array(X), np.array(Y)
+
+    def _fit(self):
+        mean, Phi, coef = self._pod()
+        self.basis, self.coef = (mean, Phi), coef
+        X, Y = self._dataset(coef)
+        xm, xs = X.mean(axis=0), X.std(axis=0)
+        ym, ys = Y.mean(axis=0), Y.std(axis=0)
+        xs = np.where(xs > 1e-12 * max(1.0, np.abs(xm).max()), xs, 1.0)
+        ys = np.where(ys > 1e-30, ys, 1.0)
+        self.norm = (xm, xs, ym, ys)
+        self.net.reset_optimizer()
+        self.last_loss = self.net.train((X - xm) / xs, (Y - ym) / ys, self.iters, self.lr)
+        self.trainings += 1
+        if self.log:
+            self.log(f"learned predictor: {len(self.X)} snapshots, {Phi.shape[1]} modes, "
+                     f"training loss {self.last_loss:.3e}")
+
+    # ---- prediction --------------------------------------------------------
+    def predict(self, k: int, x_o: np.ndarray, t: np.ndarray, dS: float, x_plain: np.ndarray):
+        if self.basis is None or len(self.X) < self.start:
+            return None
+        torch = self.torch
+        mean, Phi = self.basis
+        m = len(self.X)
+        coef = self.coef
+        f, quad = self._features(m, dS, coef)
+        xm, xs, ym, ys = self.norm
+        dy = self.net.forward(((f - xm) / xs)[None, :])[0].astype(np.float64) * ys + ym
+        a = coef[m - 1] + dS * (quad + dy)
+        r = Phi.shape[1]
+        cand = mean + Phi @ torch.from_numpy(a[:r]).to(self.dev)
+        return cand.cpu().numpy()

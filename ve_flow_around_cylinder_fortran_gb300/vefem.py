@@ -31,7 +31,10 @@ VEFEM_TIMING = 0x1000
 EXPORTED = ["vefem_abi_version", "vefem_create", "vefem_set_params", "vefem_assemble",
             "vefem_last_timing", "vefem_last_launch_count", "vefem_stream", "vefem_destroy",
             "vefem_last_error", "vefem_build_pattern", "vefem_apply_dirichlet",
-            "vefem_algorithmic_ops", "vefem_assemble_residual_noalloc"]
+            "vefem_algorithmic_ops", "vefem_assemble_residual_noalloc",
+            "vefem_mlp_create", "vefem_mlp_num_params", "vefem_mlp_set_params",
+            "vefem_mlp_get_params", "vefem_mlp_forward", "vefem_mlp_loss_grad", "vefem_mlp_train",
+            "vefem_mlp_reset_optimizer", "vefem_mlp_destroy", "vefem_mlp_last_error"]
 
 
 class VefemError(RuntimeError):
@@ -80,6 +83,19 @@ def load(path: str = LIB_PATH):
     L.vefem_last_error.restype = ctypes.c_char_p
     L.vefem_build_pattern.argtypes = [P, ctypes.c_int, P, P, P, P]
     L.vefem_apply_dirichlet.argtypes = [P, ctypes.c_int, P, P, P, P, P, ctypes.c_int, ctypes.c_int]
+    I, I64, F = ctypes.c_int, ctypes.c_int64, ctypes.c_float
+    L.vefem_mlp_create.argtypes = [I, I, I, I, ctypes.c_uint64, I, ctypes.POINTER(P)]
+    L.vefem_mlp_num_params.argtypes = [P]
+    L.vefem_mlp_num_params.restype = I64
+    L.vefem_mlp_set_params.argtypes = [P, P, I64]
+    L.vefem_mlp_get_params.argtypes = [P, P, I64]
+    L.vefem_mlp_forward.argtypes = [P, P, I, P]
+    L.vefem_mlp_loss_grad.argtypes = [P, P, P, I, P, P]
+    L.vefem_mlp_train.argtypes = [P, P, P, I, I, F, P]
+    L.vefem_mlp_reset_optimizer.argtypes = [P]
+    L.vefem_mlp_destroy.argtypes = [P]
+    L.vefem_mlp_last_error.argtypes = [P]
+    L.vefem_mlp_last_error.restype = ctypes.c_char_p
     _lib = L
     return L
 
@@ -223,6 +239,89 @@ class BulkAssembler:
     def close(self):
         if getattr(self, "_h", None):
             self._L.vefem_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class MLP:
+    """The learned predictor's network on the GPU (vefem_mlp_* in vefem.h):
+    ``in_dim -> width (GELU) x hidden -> out_dim``, BF16 weights with FP32
+    accumulation, trained by the library's own forward, backward and Adam
+    kernels.  Arrays cross the boundary as host float32."""
+
+    def __init__(self, in_dim: int, out_dim: int, width: int = 256, hidden: int = 3,
+                 seed: int = 0, device: int = 0):
+        self._L = load()
+        self.in_dim, self.out_dim, self.width, self.hidden = in_dim, out_dim, width, hidden
+        h = ctypes.c_void_p()
+        rc = self._L.vefem_mlp_create(in_dim, width, out_dim, hidden, seed, device,
+                                      ctypes.byref(h))
+        if rc:
+            raise VefemError(f"vefem_mlp_create failed ({rc}): "
+                             f"{self._L.vefem_last_error(None).decode()}")
+        self._h = h
+        self.n_params = int(self._L.vefem_mlp_num_params(h))
+
+    def _check(self, rc):
+        if rc:
+            raise VefemError(f"vefem_mlp error {rc}: {self._L.vefem_mlp_last_error(self._h).decode()}")
+
+    @staticmethod
+    def _f32(a, shape=None):
+        a = np.ascontiguousarray(a, dtype=np.float32)
+        if shape is not None and a.shape != shape:
+            raise ValueError(f"expected shape {shape}, got {a.shape}")
+        return a
+
+    def get_params(self) -> np.ndarray:
+        p = np.empty(self.n_params, np.float32)
+        self._check(self._L.vefem_mlp_get_params(self._h, p.ctypes.data, self.n_params))
+        return p
+
+    def set_params(self, p):
+        p = self._f32(p, (self.n_params,))
+        self._check(self._L.vefem_mlp_set_params(self._h, p.ctypes.data, self.n_params))
+
+    def forward(self, X) -> np.ndarray:
+        X = self._f32(X)
+        n = X.shape[0]
+        self._f32(X, (n, self.in_dim))
+        Y = np.empty((n, self.out_dim), np.float32)
+        self._check(self._L.vefem_mlp_forward(self._h, X.ctypes.data, n, Y.ctypes.data))
+        return Y
+
+    def loss_grad(self, X, T):
+        X = self._f32(X)
+        n = X.shape[0]
+        self._f32(X, (n, self.in_dim))
+        T = self._f32(T, (n, self.out_dim))
+        loss = np.zeros(1, np.float32)
+        g = np.empty(self.n_params, np.float32)
+        self._check(self._L.vefem_mlp_loss_grad(self._h, X.ctypes.data, T.ctypes.data, n,
+                                                loss.ctypes.data, g.ctypes.data))
+        return float(loss[0]), g
+
+    def train(self, X, T, iters: int, lr: float = 1e-3) -> float:
+        X = self._f32(X)
+        n = X.shape[0]
+        self._f32(X, (n, self.in_dim))
+        T = self._f32(T, (n, self.out_dim))
+        loss = np.zeros(1, np.float32)
+        self._check(self._L.vefem_mlp_train(self._h, X.ctypes.data, T.ctypes.data, n, iters,
+                                            ctypes.c_float(lr), loss.ctypes.data))
+        return float(loss[0])
+
+    def reset_optimizer(self):
+        self._check(self._L.vefem_mlp_reset_optimizer(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.vefem_mlp_destroy(self._h)
             self._h = None
 
     def __del__(self):
