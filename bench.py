@@ -17,7 +17,16 @@ unknown (Nex = 1).  Synthetic seeded state (no dataset exists for this path).
   vefem_algorithmic_ops) / its event-timed duration, peak = the FP64
   instruction rate measured live on this GPU by a probe kernel;
 * cpu_baseline: the CPU oracle (a C restatement of the reference algorithm)
-  on all host cores, on a bounded sample of the same workload.
+  on all host cores, on a bounded sample of the same workload;
+* continuation: the metric's continuation comparison, Wi 0.1 -> 1.0 by
+  pseudo-arclength on a smaller mesh (``--cont-nel``, 500 quads by default so
+  the run stays within minutes): the plain FP64 path (FD64 Jacobian, tangent
+  predictor) against the learned + mixed path (FP32 Jacobian, learned
+  predictor), wall time, steps/s, Newton iterations and LU factorisations.
+  ``--continuation-only --cont-nel N`` runs only this comparison;
+* batched: the batched form, 64 instances of 2,000-20,000 quads at Wi in
+  [0.1, 1.0], one persistent launch per kernel replayed as a CUDA graph,
+  against one call per instance.
 
 ``--impl reference`` times that CPU implementation as the reference arm.
 Multi-GPU: the assembly of one mesh does not shard across GPUs in this
@@ -60,6 +69,13 @@ def parse_args():
     ap.add_argument("--impl", choices=["vefem", "reference"], default="vefem")
     ap.add_argument("--nel", type=int, default=40000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cont-nel", type=int, default=500,
+                    help="mesh of the continuation comparison (0 = skip it)")
+    ap.add_argument("--cont-wi", type=float, default=1.0, help="Wi the continuation ends at")
+    ap.add_argument("--continuation-only", action="store_true",
+                    help="run only the continuation comparison and print its JSON line")
+    ap.add_argument("--batch-inst", type=int, default=64,
+                    help="instances of the batched-form measurement (0 = skip it)")
     return ap.parse_args()
 
 
@@ -236,12 +252,156 @@ def run_reference(args):
     return 0
 
 
+def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=None):
+    """Arclength continuation Wi 0.1 -> wi_end (Oldroyd-B, beta = 0.59, SQRT
+    form) on the GPU assembly, two arms from the same start: the plain FP64
+    path (FD64 Jacobian, tangent predictor) and the learned + mixed path
+    (FP32 exact Jacobian with FP64 residual, learned POD/MLP predictor trained
+    online after the first 20 points).  Every point is converged to
+    ||R|| < 1e-10 and ||dx|| < 1e-10; host wall time per arm."""
+    from ve_flow_around_cylinder_fortran_gb300 import continuation as C
+    from ve_flow_around_cylinder_fortran_gb300 import learned as LP
+    from ve_flow_around_cylinder_fortran_gb300 import newton as NW
+    mesh = M.build_cylinder_mesh(nel)
+    phys = S.oldroyd_b(0.1, 0.59, "SQRT", nex=1)
+    TL, EU = NW.initial_state(mesh, phys)
+    rowptr, colind = P.build_pattern(mesh.element_nodes(), mesh.nnodes, phys.nex)
+    asm = V.BulkAssembler(mesh, phys, rowptr, colind, outlet_edges=True, device=device)
+    cfg = C.ArclengthSettings(dArN=0.01, lam_max=wi_end / phys.Wi0, max_steps=2000)
+    arms, states = {}, {}
+    for name, jac, learned in (("plain_fp64", "fd64", False), ("learned_fp32", "exact32", True)):
+        cont = C.ArclengthContinuation(asm, mesh, phys, jac, cfg)
+        pred = LP.LearnedPredictor(n_modes=32, start=20, device=f"cuda:{device}") if learned else None
+        t0 = time.perf_counter()
+        recs, xs = cont.run(TL, EU, predictor=pred)
+        wall = time.perf_counter() - t0
+        if pred is not None:
+            pred.net.close()
+        states[name] = xs
+        arms[name] = {
+            "jacobian": jac, "predictor": "learned POD/MLP" if learned else "tangent",
+            "wall_s": wall, "steps": len(recs), "steps_per_s": len(recs) / wall,
+            "newton_iterations": sum(r.newton_iterations for r in recs),
+            "factorisations": sum(r.factorisations for r in recs),
+            "learned_taken": sum(r.predictor == "learned" for r in recs),
+            "emergency_restarts": sum(r.emergencies for r in recs),
+            "final_wi": recs[-1].wi, "max_final_res_norm": max(r.res_norm for r in recs),
+            "time_split_s": {"assembly": sum(r.assembly_s for r in recs),
+                             "lu_factor": sum(r.factor_s for r in recs),
+                             "lu_solve": sum(r.solve_s for r in recs),
+                             "predictor": sum(r.predictor_s for r in recs)},
+            "mean_dS_after_20": float(np.mean([r.dS for r in recs[20:]])) if len(recs) > 20 else None,
+        }
+        if pred is not None:
+            arms[name]["predictor_split_s"] = dict(pred.timers, judge=cont.judge_s)
+        if log:
+            log(f"{name}: {arms[name]}")
+    asm.close()
+    # the learned arm's points against the plain arm's branch (linear interpolation in lambda)
+    xp = states["plain_fp64"]
+    lp = np.array([x[-1] for x in xp])
+    dev = 0.0
+    for x in states["learned_fp32"][20:-1]:
+        k = int(np.searchsorted(lp, x[-1]))
+        if 0 < k < len(lp):
+            w = (x[-1] - lp[k - 1]) / (lp[k] - lp[k - 1])
+            ref = (1 - w) * xp[k - 1] + w * xp[k]
+            dev = max(dev, float(np.linalg.norm(x - ref) / np.linalg.norm(ref)))
+    return {
+        "workload": f"arclength continuation Wi 0.1 -> {wi_end}, Oldroyd-B beta=0.59, SQRT form, "
+                    f"{mesh.nel} Q2 quads ({len(rowptr) - 1} unknowns), LN0=1, dArN=0.01, "
+                    "Eps_Pr=1e-3, dS0=1, dS_max=50; host SuperLU (nested dissection) solve",
+        "arms": arms,
+        "speedup_wall": arms["plain_fp64"]["wall_s"] / arms["learned_fp32"]["wall_s"],
+        "speedup_factorisations": arms["plain_fp64"]["factorisations"]
+        / max(1, arms["learned_fp32"]["factorisations"]),
+        "branch_max_rel_dev": dev,
+    }
+
+
+def batched_compare(ninst: int, steps: int, warmup: int, device: int = 0, seed: int = 0):
+    """Batched form: ninst Oldroyd-B instances (beta = 0.59, SQRT form), Wi
+    uniform in [0.1, 1.0], meshes of 2,000-20,000 quads drawn log-uniformly
+    (nearest block layout), seeded states; FP64 residual + FP32 Jacobian per
+    step, all instances in one persistent launch per kernel replayed as a
+    CUDA graph, tiles from the autotuner -- against one vefem_assemble per
+    instance on the same device buffers."""
+    import torch
+    rng = np.random.default_rng(seed)
+    sizes = np.round(np.exp(rng.uniform(np.log(2000), np.log(20000), ninst))).astype(int)
+    wis = rng.uniform(0.1, 1.0, ninst)
+    meshes, physs, pats, TLs, EUs = [], [], [], [], []
+    d = torch.device(f"cuda:{device}")
+    for k in range(ninst):
+        m = M.build_cylinder_mesh(int(sizes[k]), exact=False)
+        p = S.oldroyd_b(float(wis[k]), 0.59, "SQRT", nex=0)
+        TL, _ = S.seeded_state(m.xyz, p, seed=k)
+        meshes.append(m)
+        physs.append(p)
+        pats.append(V.build_pattern(m.conn, m.nnodes, 0))
+        TLs.append(torch.from_numpy(TL).to(d))
+        EUs.append(torch.zeros(1, dtype=torch.float64, device=d))
+    bs = [torch.zeros(len(rp) - 1, dtype=torch.float64, device=d) for rp, _ in pats]
+    vs = [torch.zeros(len(ci), dtype=torch.float32, device=d) for _, ci in pats]
+    nel = int(sum(m.nel for m in meshes))
+    flags = V.VEFEM_RESIDUAL | V.VEFEM_JAC_EXACT32 | V.VEFEM_ZERO_FIRST
+    bt = V.BatchAssembler(meshes, physs, pats, device=device)
+    t0 = time.perf_counter()
+    tiles = bt.autotune(flags, reps=2)
+    tune_s = time.perf_counter() - t0
+    for _ in range(warmup):
+        bt.assemble(TLs, EUs, flags, bs, vs, on_device=True)
+    bt.assemble(TLs, EUs, flags | V.VEFEM_TIMING, bs, vs, on_device=True)
+    tm = bt.last_timing()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        bt.assemble(TLs, EUs, flags, bs, vs, on_device=True)
+    torch.cuda.synchronize()
+    bat_s = time.perf_counter() - t0
+    info = bt.info()
+    bt.close()
+    singles = [V.BulkAssembler(m, p, rp, ci, device=device) for m, p, (rp, ci) in zip(meshes, physs, pats)]
+    for _ in range(warmup):
+        for a, TL, b, v in zip(singles, TLs, bs, vs):
+            a.assemble(TL, None, flags, b, v, on_device=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for a, TL, b, v in zip(singles, TLs, bs, vs):
+            a.assemble(TL, None, flags, b, v, on_device=True)
+    torch.cuda.synchronize()
+    seq_s = time.perf_counter() - t0
+    for a in singles:
+        a.close()
+    return {
+        "workload": f"{ninst} Oldroyd-B instances (beta=0.59, SQRT form, Nex=0), Wi ~ U[0.1,1.0], "
+                    f"{int(sizes.min())}-{int(sizes.max())} quads drawn log-uniformly in "
+                    "[2000, 20000] (nearest block layout), seeded states; FP64 residual + FP32 "
+                    "exact Jacobian into AIJ",
+        "elements": nel, "value": nel * steps / bat_s, "unit": UNIT,
+        "ms_per_step": 1e3 * bat_s / steps,
+        "sequential_value": nel * steps / seq_s, "speedup_vs_sequential": seq_s / bat_s,
+        "element_kernels_ms": tm[0], "scatter_ms": tm[1], "zeroing_ms": tm[2],
+        "tiles_by_size_class": tiles, "autotune_s": tune_s, "work_items": info["work_items"],
+        "grid": info["grid"], "launches_per_step": info["launches"],
+        "timing": "host clock around graph replays, each call synchronised",
+    }
+
+
 def run_vefem(args):
     import torch
     world, rank, local, dist = dist_setup()
     dev = local
     torch.cuda.set_device(dev)
     B.build()
+    if args.continuation_only:
+        if rank == 0:
+            out = continuation_compare(args.cont_nel, args.cont_wi, dev)
+            print(json.dumps({"continuation": out}))
+        if dist:
+            dist.destroy_process_group()
+        return 0
     mesh, phys, TL, EU, rowptr, colind, cfg = workload(args.nel)
     asm = V.BulkAssembler(mesh, phys, rowptr, colind, device=dev)
     nel = mesh.nel
@@ -383,8 +543,12 @@ def run_vefem(args):
                           "kernel_ms_avg": statistics.mean(r_k)},
     }
     line.update(forms)
-    print(json.dumps(line))
     asm.close()
+    if world == 1 and args.batch_inst > 0:
+        line["batched"] = batched_compare(args.batch_inst, max(3, args.steps // 2), args.warmup, dev)
+    if world == 1 and args.cont_nel > 0:
+        line["continuation"] = continuation_compare(args.cont_nel, args.cont_wi, dev)
+    print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
     return 0

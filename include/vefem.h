@@ -197,6 +197,44 @@ int vefem_assemble_residual_noalloc(const vefem_params *params, int nnodes, int 
 
 int vefem_abi_version(void);
 
+/* ---- Batched form ---------------------------------------------------------
+ * Many independent instances (Weissenberg points, meshes of uneven size)
+ * assembled by one persistent launch per kernel, replayed as a CUDA graph.
+ * Each instance is what one vefem_create would take; the batched call is
+ * setEquationsBulk (Equations_mod.F90:21-55) for every instance at once,
+ * with the same ADD semantics and bit-identical results to one
+ * vefem_assemble per instance.  All instances must share the device, the
+ * conformation form and the zero/non-zero pattern of ReN and DfN.
+ * Flags: VEFEM_RESIDUAL, VEFEM_JAC_EXACT32 or VEFEM_JAC_EXACT64,
+ * VEFEM_ZERO_FIRST, VEFEM_TIMING (VEFEM_JAC_FD64 and VEFEM_OUTLET_EDGES are
+ * VEFEM_ERR_UNSUPPORTED here: the outlet edges are the separate reference
+ * call setEquationsEdge).  Arrays of pointers, one per instance; vals are
+ * double for EXACT64 and float for EXACT32.  With on_device = 1 the first
+ * call for a flag set captures a CUDA graph, later calls replay it. */
+typedef struct vefem_batch vefem_batch;
+
+int vefem_batch_create(int ninst, const vefem_mesh *meshes, const vefem_csr *patterns,
+                       const vefem_params *params, vefem_batch **out);
+int vefem_batch_set_params(vefem_batch *bt, int inst, const vefem_params *params);
+int vefem_assemble_batched(vefem_batch *bt, const double *const *TL, const double *const *EU,
+                           int flags, double *const *b, void *const *vals, int on_device);
+/* Element-batch tile per mesh-size class (class c: nel in [1000*2^c, 1000*2^(c+1)),
+ * c clamped to 0..VEFEM_BATCH_CLASSES-1).  vefem_batch_autotune times every
+ * candidate tile of every class present on the live GPU (reps launches each,
+ * device-resident buffers of its own) and keeps the fastest; tiles_out
+ * (may be NULL) receives the chosen tiles. */
+#define VEFEM_BATCH_CLASSES 6
+int vefem_batch_autotune(vefem_batch *bt, int flags, int reps, int *tiles_out);
+int vefem_batch_set_tiles(vefem_batch *bt, const int *tiles);
+/* out[0] instances, out[1] elements, out[2] work items of the Jacobian kernel,
+ * out[3] its persistent grid, out[4] kernels launched by the last call,
+ * out[5] graph replays so far */
+int vefem_batch_info(const vefem_batch *bt, int64_t out[6]);
+/* with VEFEM_TIMING: ms[0] element kernels, ms[1] scatter, ms[2] copies and zeroing */
+int vefem_batch_last_timing(const vefem_batch *bt, float ms[3]);
+int vefem_batch_destroy(vefem_batch *bt);
+const char *vefem_batch_last_error(const vefem_batch *bt);
+
 /* ---- Learned continuation predictor: network kernels ---------------------
  * No counterpart in the reference (its arclength predictor is the tangent
  * step of updateSolutionArclength, Continuation_Arclength_mod.F90:339-379).

@@ -17,7 +17,10 @@ Nex = 1 (the extra unknown lambda, Wi = Wi0 * lambda at every Gauss point):
 * adjustContinuationStep (:282-337): err_pr = max over fields of
   |x - x_p| / |x|, trns = sqrt(Eps_Pr / err_pr) capped at 2,
   dS = min(dS trns, dS_max);
-* updateSolutionArclength (:339-379): the plain predictor x_p = x + t dS.
+* updateSolutionArclength (:339-379): the plain predictor x_p = x + t dS;
+* emergencyNewtonRaphson (Newton_Raphson_mod.F90:533-584) when Newton
+  diverges: restart from the prediction with the relaxation halved, 50 x
+  Niter iterations and dSo halved.
 
 A predictor object can replace the plain prediction (the learned POD/MLP
 predictor in ``learned.py``); Newton stays the corrector.  The host solves
@@ -64,6 +67,11 @@ class StepRecord:
     predictor: str
     pred_error: float
     wall_s: float
+    assembly_s: float = 0.0     # device assembly + Dirichlet/lambda rows, host copies
+    factor_s: float = 0.0       # host LU factorisations
+    solve_s: float = 0.0        # host triangular solves (Newton and tangent)
+    predictor_s: float = 0.0    # learned predictor: prediction, judging, training
+    emergencies: int = 0        # Newton restarts with relaxation (emergencyNewtonRaphson)
 
 
 class LambdaRow:
@@ -116,6 +124,7 @@ class ArclengthContinuation:
         self.solver = LS.SparseLU(asm.rowptr, asm.colind, mesh)
         self.N = asm.N
         self.nn = asm.nnodes
+        self.judge_s = 0.0
 
     # state vector x = [TL in node-major order, lambda]
     def pack(self, TL, EU):
@@ -130,11 +139,12 @@ class ArclengthContinuation:
         rows, values = NW.boundary_conditions(self.mesh, p)
         self.dev.set_values(values)
 
-    def _newton(self, x0: np.ndarray):
-        """Newton with the lambda row; returns (x, iterations, factorisations,
-        last residual norm, last LU or None)."""
+    def _newton(self, x0: np.ndarray, xF: float = 1.0, max_iter: int = NW.NITER):
+        """Newton with the lambda row and relaxation xF; returns (x, iterations,
+        factorisations, last residual norm, last LU, converged)."""
         cfg = self.cfg
         x = x0.copy()
+        tm = self.timers
         res_norm = cor_new = cor_old = 1.0
         flag = "NRP"
         lu = None
@@ -145,27 +155,34 @@ class ArclengthContinuation:
             it += 1
             if it % 10 == 0:
                 flag = "NRP"
+            t0 = time.perf_counter()
             TL, EU = self.unpack(x)
             want = flag == "NRP" or lu is None
             self._update_inflow(float(EU[0]))
             b, vals = self.dev(TL, EU, want)
             self.lrow(x, b, vals)
             res_norm = float(np.linalg.norm(b))
+            t1 = time.perf_counter()
             if want:
                 lu = self.solver.factor(vals)
                 nfac += 1
+            t2 = time.perf_counter()
             s = lu.solve(b)
+            t3 = time.perf_counter()
+            tm["assembly"] += t1 - t0
+            tm["factor"] += t2 - t1
+            tm["solve"] += t3 - t2
             cor_new = float(np.linalg.norm(s))
             if self.log:
                 self.log(f"   {it:3d}. {flag}: RES_NORM = {res_norm:.4e}, COR_NORM = {cor_new:.4e}")
-            if cor_new != cor_new or cor_new > NW.COR_NORM_DIV or it > NW.NITER:
+            if cor_new != cor_new or cor_new > NW.COR_NORM_DIV or it > max_iter:
                 return x, it, nfac, res_norm, lu, False
             if flag == "NRP":
                 flag = "MNR" if cor_new < NW.MNR_EPS else "NRP"
             else:
                 flag = "NRP" if cor_new > cor_old else "MNR"
             cor_old = cor_new
-            x = x - s
+            x = x - xF * s
 
     def run(self, TL0: np.ndarray, EU0: np.ndarray, predictor=None):
         """Continue from (TL0, EU0) until lambda >= lam_max; returns the step
@@ -179,6 +196,7 @@ class ArclengthContinuation:
         records, states = [], []
         for k in range(1, cfg.max_steps + 1):
             t0 = time.perf_counter()
+            self.timers = dict(assembly=0.0, factor=0.0, solve=0.0, predictor=0.0)
             if k <= 2:
                 self.lrow.mode = "pinned"
                 self.lrow.target = cfg.LN0 + (k - 1) * cfg.dArN
@@ -188,12 +206,30 @@ class ArclengthContinuation:
                 self.lrow.t, self.lrow.x_o, self.lrow.dS = t, x_o, dS
             pred_name = "plain"
             if predictor is not None and k > 2:
+                tp = time.perf_counter()
                 cand = predictor.predict(k, x_o, t, dS, x_p)
                 if cand is not None:
                     x_p, pred_name = self._judge(x_p, cand)
-            x, its, nfac, rn, lu, ok = self._newton(x_p)
-            if not ok:
-                raise RuntimeError(f"arclength Newton failed at increment {k}")
+                self.timers["predictor"] += time.perf_counter() - tp
+            # emergencyNewtonRaphson (Newton_Raphson_mod.F90:533-584): restart
+            # from the prediction with the relaxation halved, 50 x Niter
+            # iterations allowed and, on the arclength branch, dSo halved
+            xF, max_it, its, nfac, emerg = 1.0, NW.NITER, 0, 0, 0
+            while True:
+                x, i1, f1, rn, lu, ok = self._newton(x_p, xF, max_it)
+                its += i1
+                nfac += f1
+                if ok:
+                    break
+                xF *= 0.5
+                emerg += 1
+                if xF < 1.0e-2:
+                    raise RuntimeError(f"arclength Newton failed at increment {k} "
+                                       f"(lambda = {x_p[-1]:.6g}, dS = {dS:.4g})")
+                max_it = 50 * NW.NITER
+                if k > 2:
+                    dS *= 0.5
+                    self.lrow.dS = dS
             err_pr = 0.0
             if k > 1:
                 TLc, EUc = self.unpack(x)
@@ -203,30 +239,37 @@ class ArclengthContinuation:
                 e.append(abs(EUc[0] - EUp[0]) / max(abs(EUc[0]), 1e-300))
                 err_pr = max(e)
             lam = float(x[-1])
-            wall = time.perf_counter() - t0
-            records.append(StepRecord(k, self.phys.Wi0 * lam, lam, dS, its, nfac, rn, pred_name,
-                                      err_pr, wall))
-            states.append(x.copy())
-            if self.log:
-                self.log(f"step {k}: Wi = {self.phys.Wi0 * lam:.4f}, Newton {its}, "
-                         f"pred {pred_name} err {err_pr:.2e}, dS = {dS:.3f}, {wall:.2f} s")
             if predictor is not None:
+                tp = time.perf_counter()
                 predictor.observe(k, x, self.phys.Wi0 * lam)
-            if lam >= cfg.lam_max:
-                break
+                self.timers["predictor"] += time.perf_counter() - tp
+            states.append(x.copy())
+            done = lam >= cfg.lam_max
             # direction (setDirectionVectors)
             if k == 1:
                 t_new = None
             elif k == 2:
                 d = x - x_o
                 t_new = d / np.linalg.norm(d)
-            else:
+            elif not done:
                 e_l = np.zeros(self.N)
                 e_l[-1] = 1.0
+                ts = time.perf_counter()
                 tv = lu.solve(e_l)
+                self.timers["solve"] += time.perf_counter() - ts
                 t_new = tv / np.linalg.norm(tv)
                 if np.dot(t_new, t) < 0.0:
                     t_new = -t_new
+            wall = time.perf_counter() - t0
+            tm = self.timers
+            records.append(StepRecord(k, self.phys.Wi0 * lam, lam, dS, its, nfac, rn, pred_name,
+                                      err_pr, wall, tm["assembly"], tm["factor"], tm["solve"],
+                                      tm["predictor"], emerg))
+            if self.log:
+                self.log(f"step {k}: Wi = {self.phys.Wi0 * lam:.4f}, Newton {its}, "
+                         f"pred {pred_name} err {err_pr:.2e}, dS = {dS:.3f}, {wall:.2f} s")
+            if done:
+                break
             # step size (adjustContinuationStep)
             if k > 1:
                 trns = min(np.sqrt(cfg.eps_pr / max(err_pr, 1e-300)), 2.0)
@@ -240,6 +283,7 @@ class ArclengthContinuation:
     def _judge(self, x_plain, x_cand):
         """Newton judges the learned prediction by residual norm: the candidate
         is used only when its residual is smaller than the plain prediction's."""
+        t0 = time.perf_counter()
         r = []
         for x in (x_plain, x_cand):
             TL, EU = self.unpack(x)
@@ -247,6 +291,7 @@ class ArclengthContinuation:
             b, _ = self.dev(TL, EU, False)
             self.lrow(x, b, None)
             r.append(float(np.linalg.norm(b)))
+        self.judge_s += time.perf_counter() - t0
         if r[1] < r[0]:
             return x_cand, "learned"
         return x_plain, "plain"

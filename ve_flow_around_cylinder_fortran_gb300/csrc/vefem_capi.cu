@@ -22,40 +22,10 @@
 #include <vector>
 
 #include "vefem.h"
+#include "vefem_ctx.h"
 #include "vefem_internal.h"
 
 using namespace vefem;
-
-struct vefem_ctx {
-    int device = 0;
-    int nnodes = 0, nel = 0, nex = 0;
-    int64_t N = 0, nnz = 0;
-    int nblocks = 0;
-    int nedge = 0;
-    KParams prm{};
-    cudaStream_t stream = nullptr;
-    cudaEvent_t ev[8] = {};
-    float timing[5] = {0, 0, 0, 0, 0};
-    int launches = 0;
-    std::string err;
-    // device tables
-    int32_t *d_conn = nullptr;
-    double *d_xy = nullptr;
-    int64_t *d_rowptr = nullptr;
-    int32_t *d_nptr = nullptr, *d_ncon = nullptr;
-    int32_t *d_brow = nullptr, *d_boff = nullptr, *d_bptr = nullptr, *d_bcon = nullptr;
-    int32_t *d_edge_elem = nullptr, *d_edge_id = nullptr;
-    int32_t *d_edge_row = nullptr, *d_edge_off = nullptr;   // [nedge][81]
-    int32_t *d_colind = nullptr;                            // for MatZeroRows on the device
-    std::vector<int64_t> h_rowptr;                          // host copies for host-side rows
-    std::vector<int32_t> h_colind;
-    // device scratch / staging (allocated on first use)
-    double *d_rs = nullptr, *d_es = nullptr, *d_as = nullptr;
-    float *d_es32 = nullptr, *d_as32 = nullptr;
-    float *d_vals32 = nullptr;
-    double *d_ers = nullptr, *d_ees = nullptr, *d_eas = nullptr;
-    double *d_TL = nullptr, *d_EU = nullptr, *d_b = nullptr, *d_vals = nullptr;
-};
 
 static std::string g_create_error;
 
@@ -579,11 +549,28 @@ extern "C" int vefem_assemble(vefem_ctx *ctx, const double *TL, const double *EU
             CK(launch_residual64(ea, ctx->prm, s));
             ctx->launches++;
         }
-        if (jmode == VEFEM_JAC_EXACT64) {
-            CK(launch_exact<double>(ea, ctx->prm, ctx->d_es, ctx->d_as, s));
-            ctx->launches++;
-        } else if (jac32) {
-            CK(launch_exact<float>(ea, ctx->prm, ctx->d_es32, ctx->d_as32, s));
+        if (jmode == VEFEM_JAC_EXACT64 || jac32) {
+            if (!ctx->d_self) {
+                CK(cudaMalloc((void **)&ctx->d_self, sizeof(BatchInst)));
+                std::vector<WorkItem> w(nel);
+                for (int e = 0; e < (int)nel; e++) w[e] = {0, e, 1, 0};
+                CK(cudaMalloc((void **)&ctx->d_work, nel * sizeof(WorkItem)));
+                CK(cudaMemcpy(ctx->d_work, w.data(), nel * sizeof(WorkItem), cudaMemcpyHostToDevice));
+                CK(cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, ctx->device));
+            }
+            BatchInst &I = ctx->h_self;
+            I.ea = ea;
+            I.prm = ctx->prm;
+            I.es = jac32 ? (void *)ctx->d_es32 : (void *)ctx->d_es;
+            I.as = jac32 ? (void *)ctx->d_as32 : (void *)ctx->d_as;
+            CK(cudaMemcpyAsync(ctx->d_self, &I, sizeof(BatchInst), cudaMemcpyHostToDevice, s));
+            const int spec = (ctx->prm.ReN == 0.0 ? SPEC_RE0 : 0) | (ctx->prm.DfN == 0.0 ? SPEC_DF0 : 0);
+            const int occ = exact_batched_ctas_per_sm(jac32 ? 4 : 8, ctx->prm.form, spec);
+            const int grid = std::min<int>((int)nel, ctx->sms * std::max(1, occ));
+            if (jac32)
+                CK(launch_exact_batched<float>(ctx->d_self, ctx->d_work, (int)nel, ctx->prm.form, spec, grid, s));
+            else
+                CK(launch_exact_batched<double>(ctx->d_self, ctx->d_work, (int)nel, ctx->prm.form, spec, grid, s));
             ctx->launches++;
         }
     }
@@ -736,7 +723,8 @@ extern "C" int vefem_destroy(vefem_ctx *ctx)
                     ctx->d_boff, ctx->d_bptr, ctx->d_bcon, ctx->d_edge_elem, ctx->d_edge_id,
                     ctx->d_edge_row, ctx->d_edge_off, ctx->d_rs, ctx->d_es, ctx->d_as,
                     ctx->d_ers, ctx->d_ees, ctx->d_eas, ctx->d_TL, ctx->d_EU, ctx->d_b,
-                    ctx->d_vals, ctx->d_es32, ctx->d_as32, ctx->d_vals32, ctx->d_colind};
+                    ctx->d_vals, ctx->d_es32, ctx->d_as32, ctx->d_vals32, ctx->d_colind,
+                    ctx->d_self, ctx->d_work};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int i = 0; i < 8; i++)

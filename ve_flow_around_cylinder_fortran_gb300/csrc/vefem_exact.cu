@@ -14,7 +14,9 @@
 // This replaces the 56 residual evaluations of the forward difference; it is
 // the derivative the FD approximates (they differ by the FD truncation error).
 //
-// One CTA per element, 192 threads:
+// One element at a time per CTA of 192 threads (persistent: each CTA walks a
+// list of work items, each a run of consecutive elements of one mesh; a
+// single mesh is the one-instance case):
 //   phase 0  state and geometry (geometry in FP64, stored in T);
 //   phase 1  thread (gp, d): D[gp][d][e*3+k] = dc_ek/dq_d;
 //   phase 2a A[gp][d][i*6+e] = WET sum_k psi_k(i) D[gp][d][e*3+k];
@@ -71,8 +73,8 @@ struct TView {
 };
 
 template <class T, int FORM, int SPEC>
-__global__ void __launch_bounds__(EX_THREADS)
-k_exact(const ElemArgs a, const KParams prm, T *__restrict__ es, T *__restrict__ as)
+__device__ __forceinline__ void exact_element(const ElemArgs &a, const KParams &prm,
+                                              T *__restrict__ es, T *__restrict__ as, const int e)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
     T *D = reinterpret_cast<T *>(smraw);               // [9][21][18]
@@ -80,7 +82,6 @@ k_exact(const ElemArgs a, const KParams prm, T *__restrict__ es, T *__restrict__
     __shared__ T s_tl[54];
     __shared__ T s_dFx[9][9], s_dFy[9][9], s_d2x[9][9], s_d2y[9][9], s_lap[9][9];
     __shared__ T s_H2[9], s_WET[9];
-    const int e = blockIdx.x;
     const int t = threadIdx.x;
 
     if (t < 54) {
@@ -188,40 +189,79 @@ k_exact(const ElemArgs a, const KParams prm, T *__restrict__ es, T *__restrict__
     }
 }
 
-template <class T, int FORM>
-static cudaError_t launch_exact_form(const ElemArgs &a, const KParams &p, T *es, T *as,
-                                     cudaStream_t s)
+// persistent form over the work items of many meshes; each item is a run of
+// consecutive elements of one mesh (the element-batch tile of its size class)
+template <class T, int FORM, int SPEC>
+__global__ void __launch_bounds__(EX_THREADS)
+k_exact_batched(const BatchInst *__restrict__ insts, const WorkItem *__restrict__ work, int nwork)
 {
-    const int spec = (p.ReN == 0.0 ? SPEC_RE0 : 0) | (p.DfN == 0.0 ? SPEC_DF0 : 0);
-    const size_t smem = sizeof(T) * (9 * EX_NDIR * 18 + 9 * EX_NDIR * 54);
-    cudaError_t e = cudaSuccess;
-#define GO(SP)                                                                             \
-    e = cudaFuncSetAttribute(k_exact<T, FORM, SP>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                             (int)smem);                                                   \
-    if (e == cudaSuccess) k_exact<T, FORM, SP><<<a.nel, EX_THREADS, smem, s>>>(a, p, es, as);
-    switch (spec) {
-    case 0: GO(0) break;
-    case SPEC_RE0: GO(SPEC_RE0) break;
-    case SPEC_DF0: GO(SPEC_DF0) break;
-    default: GO(SPEC_RE0 | SPEC_DF0) break;
+    for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+        const WorkItem it = work[w];
+        const ElemArgs a = insts[it.inst].ea;
+        const KParams prm = insts[it.inst].prm;
+        T *es = static_cast<T *>(insts[it.inst].es);
+        T *as = static_cast<T *>(insts[it.inst].as);
+        const int e_end = min(it.e0 + it.count, a.nel);
+        for (int e = it.e0; e < e_end; e++) {
+            exact_element<T, FORM, SPEC>(a, prm, es, as, e);
+            __syncthreads();
+        }
     }
-#undef GO
+}
+
+template <class T, int FORM, int SPEC>
+static cudaError_t go_exact_batched(const BatchInst *insts, const WorkItem *work, int nwork,
+                                    int grid, cudaStream_t s)
+{
+    const size_t smem = sizeof(T) * (9 * EX_NDIR * 18 + 9 * EX_NDIR * 54);
+    cudaError_t e = cudaFuncSetAttribute(k_exact_batched<T, FORM, SPEC>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
+    k_exact_batched<T, FORM, SPEC><<<grid, EX_THREADS, smem, s>>>(insts, work, nwork);
     return cudaGetLastError();
 }
 
 template <class T>
-cudaError_t launch_exact(const ElemArgs &a, const KParams &p, T *es, T *as, cudaStream_t s)
+cudaError_t launch_exact_batched(const BatchInst *insts, const WorkItem *work, int nwork,
+                                 int form, int spec, int grid, cudaStream_t s)
 {
-    if (a.nel <= 0) return cudaSuccess;
-    if (p.form == FORM_SQRT) return launch_exact_form<T, FORM_SQRT>(a, p, es, as, s);
-    return launch_exact_form<T, FORM_T>(a, p, es, as, s);
+    if (nwork <= 0) return cudaSuccess;
+#define GO(F, SP)                                                                              if (form == F && spec == SP) return go_exact_batched<T, F, SP>(insts, work, nwork, grid, s);
+    GO(FORM_T, 0) GO(FORM_T, SPEC_RE0) GO(FORM_T, SPEC_DF0) GO(FORM_T, SPEC_RE0 | SPEC_DF0)
+    GO(FORM_SQRT, 0) GO(FORM_SQRT, SPEC_RE0) GO(FORM_SQRT, SPEC_DF0)
+    GO(FORM_SQRT, SPEC_RE0 | SPEC_DF0)
+#undef GO
+    return cudaErrorInvalidValue;
 }
 
-template cudaError_t launch_exact<float>(const ElemArgs &, const KParams &, float *, float *,
-                                         cudaStream_t);
-template cudaError_t launch_exact<double>(const ElemArgs &, const KParams &, double *, double *,
-                                          cudaStream_t);
+template <class T, int FORM, int SPEC>
+static int occ_exact()
+{
+    const size_t smem = sizeof(T) * (9 * EX_NDIR * 18 + 9 * EX_NDIR * 54);
+    if (cudaFuncSetAttribute(k_exact_batched<T, FORM, SPEC>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return 0;
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_exact_batched<T, FORM, SPEC>, EX_THREADS,
+                                                  smem);
+    return n;
+}
+
+int exact_batched_ctas_per_sm(int elem_size, int form, int spec)
+{
+#define OC(F, SP)                                                                              if (form == F && spec == SP)                                                                   return elem_size == 4 ? occ_exact<float, F, SP>() : occ_exact<double, F, SP>();
+    OC(FORM_T, 0) OC(FORM_T, SPEC_RE0) OC(FORM_T, SPEC_DF0) OC(FORM_T, SPEC_RE0 | SPEC_DF0)
+    OC(FORM_SQRT, 0) OC(FORM_SQRT, SPEC_RE0) OC(FORM_SQRT, SPEC_DF0)
+    OC(FORM_SQRT, SPEC_RE0 | SPEC_DF0)
+#undef OC
+    return 0;
+}
+
+template cudaError_t launch_exact_batched<float>(const BatchInst *, const WorkItem *, int, int,
+                                                 int, int, cudaStream_t);
+template cudaError_t launch_exact_batched<double>(const BatchInst *, const WorkItem *, int, int,
+                                                  int, int, cudaStream_t);
+
 
 // FP32 scatter of the exact Jacobian (element order, as the FP64 one)
 __global__ void k_gather_jacobian32(const GatherArgs g, const float *__restrict__ es,

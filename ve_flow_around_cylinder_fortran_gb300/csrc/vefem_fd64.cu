@@ -241,21 +241,24 @@ __global__ void __launch_bounds__(FD_THREADS) k_fd64(const ElemArgs a, const KPa
 constexpr int RS_EPB = 8;
 constexpr int RS_THREADS = RS_EPB * 9;   // 72
 
+// elements [e0, e0 + count) of one mesh, count <= RS_EPB
 template <int FORM>
-__global__ void __launch_bounds__(RS_THREADS) k_res64(const ElemArgs a, const KParams prm)
+__device__ __forceinline__ void res64_block(const ElemArgs &a, const KParams &prm, int e0,
+                                            int count)
 {
     __shared__ double s_tl[RS_EPB][54];
     __shared__ double s_part[RS_EPB][9][54];
     const int t = threadIdx.x;
     const int el = t / 9;
     const int ig = t - el * 9;
-    const int e = blockIdx.x * RS_EPB + el;
-    const bool live = (t < RS_THREADS) && e < a.nel;
+    const int e = e0 + el;
+    const int e_end = min(e0 + count, a.nel);
+    const bool live = (t < RS_THREADS) && e < e_end;
     // stage element states: 54 values per element, spread over the CTA
     for (int i = t; i < RS_EPB * 54; i += blockDim.x) {
-        const int ee = blockIdx.x * RS_EPB + i / 54;
+        const int ee = e0 + i / 54;
         const int pos = i - (i / 54) * 54;
-        if (ee < a.nel) {
+        if (ee < e_end) {
             const int inod = pos / 6, f = pos - 6 * (pos / 6);
             s_tl[i / 54][pos] = a.TL[(size_t)f * a.nnodes + a.conn[inod * a.nel + ee]];
         }
@@ -286,12 +289,32 @@ __global__ void __launch_bounds__(RS_THREADS) k_res64(const ElemArgs a, const KP
     // in-order sum over the Gauss points (Res = Res + TERM*WET, ig = 1..9)
     for (int i = t; i < RS_EPB * 54; i += blockDim.x) {
         const int le = i / 54, pos = i - (i / 54) * 54;
-        const int ee = blockIdx.x * RS_EPB + le;
-        if (ee >= a.nel) continue;
+        const int ee = e0 + le;
+        if (ee >= e_end) continue;
         double s = 0.0;
 #pragma unroll
         for (int q = 0; q < 9; q++) s = s + s_part[le][q][pos];
         a.rs[(size_t)ee * 54 + pos] = s;
+    }
+}
+
+template <int FORM>
+__global__ void __launch_bounds__(RS_THREADS) k_res64(const ElemArgs a, const KParams prm)
+{
+    res64_block<FORM>(a, prm, blockIdx.x * RS_EPB, RS_EPB);
+}
+
+// persistent form over the work items of many meshes
+template <int FORM>
+__global__ void __launch_bounds__(RS_THREADS)
+k_res64_batched(const BatchInst *__restrict__ insts, const WorkItem *__restrict__ work, int nwork)
+{
+    for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+        const WorkItem it = work[w];
+        const ElemArgs a = insts[it.inst].ea;
+        const KParams prm = insts[it.inst].prm;
+        res64_block<FORM>(a, prm, it.e0, it.count);
+        __syncthreads();
     }
 }
 
@@ -304,6 +327,27 @@ cudaError_t launch_residual64(const ElemArgs &a, const KParams &p, cudaStream_t 
     else
         k_res64<FORM_T><<<grid, RS_THREADS, 0, s>>>(a, p);
     return cudaGetLastError();
+}
+
+cudaError_t launch_residual64_batched(const BatchInst *insts, const WorkItem *work, int nwork,
+                                      int form, int grid, cudaStream_t s)
+{
+    if (nwork <= 0) return cudaSuccess;
+    if (form == FORM_SQRT)
+        k_res64_batched<FORM_SQRT><<<grid, RS_THREADS, 0, s>>>(insts, work, nwork);
+    else
+        k_res64_batched<FORM_T><<<grid, RS_THREADS, 0, s>>>(insts, work, nwork);
+    return cudaGetLastError();
+}
+
+int residual_batched_ctas_per_sm(int form)
+{
+    int n = 0;
+    if (form == FORM_SQRT)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_res64_batched<FORM_SQRT>, RS_THREADS, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_res64_batched<FORM_T>, RS_THREADS, 0);
+    return n;
 }
 
 template <int FORM>

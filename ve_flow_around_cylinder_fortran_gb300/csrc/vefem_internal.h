@@ -9,6 +9,14 @@
 
 namespace vefem {
 
+enum { FORM_T = 0, FORM_SQRT = 1 };
+
+// Specialisations that leave out terms which are exact zeros for the given
+// parameters; a sum that drops an exact-zero addend keeps its value, so the
+// results are the same as the general code (up to the sign of a zero result).
+enum { SPEC_RE0 = 1,   // ReN == 0: convection, LSME-momentum and (ReN/dt, ReN*tsugn) terms
+       SPEC_DF0 = 2 }; // DfN == 0: stress diffusion terms and DfN/Helem^2
+
 // Physics parameters as the kernels read them (one copy per launch, by value).
 struct KParams {
     int model, form, nex;
@@ -76,10 +84,9 @@ cudaError_t launch_gather_jacobian(const GatherArgs &g, const double *es, double
 cudaError_t launch_gather_arclength(const GatherArgs &g, const double *as, double *vals,
                                     cudaStream_t s);
 
-// Exact-Jacobian kernels (vefem_exact.cu): element Jacobian and arclength column in T.
+// Exact-Jacobian kernels (vefem_exact.cu): element Jacobian and arclength column in T,
+// launched through launch_exact_batched (declared below with the batched form).
 cudaError_t upload_tables_exact(const GaussTables &t, cudaStream_t s);
-template <class T>
-cudaError_t launch_exact(const ElemArgs &a, const KParams &p, T *es, T *as, cudaStream_t s);
 cudaError_t launch_gather_jacobian32(const GatherArgs &g, const float *es, float *vals,
                                      cudaStream_t s);
 cudaError_t launch_gather_arclength32(const GatherArgs &g, const float *as, float *vals,
@@ -91,5 +98,41 @@ cudaError_t launch_dirichlet(int nrows, int nnodes, const int64_t *rows, const d
 
 // Message returned by vefem_last_error(NULL) for entry points without a context.
 void set_global_error(const std::string &msg);
+
+// ---- Batched form: many instances (mesh, pattern, parameters) in one launch.
+// One descriptor per instance in device memory; the persistent kernels walk a
+// list of work items (instance, first element, element count) with a grid
+// stride.  FORM and the specialisation must be the same for all instances.
+struct BatchInst {
+    ElemArgs ea;          // element side (TL, EU, rs set per call)
+    KParams prm;
+    GatherArgs ga;
+    void *es, *as;        // element Jacobian / arclength scratch (T of the launch)
+    double *b;            // residual (device)
+    void *vals;           // AIJ values (T of the launch)
+    int64_t row0;         // first residual row of this instance in the row space (nnodes*6)
+    int64_t blk0;         // first block entry of this instance (nblocks*36)
+};
+struct WorkItem {
+    int inst, e0, count, pad;
+};
+cudaError_t launch_residual64_batched(const BatchInst *insts, const WorkItem *work, int nwork,
+                                      int form, int grid, cudaStream_t s);
+template <class T>
+cudaError_t launch_exact_batched(const BatchInst *insts, const WorkItem *work, int nwork,
+                                 int form, int spec, int grid, cudaStream_t s);
+// residual rows / block entries / arclength rows of all instances:
+// total = sum over instances; offsets [ninst + 1] are row0 (or blk0) prefixes
+cudaError_t launch_gather_residual_batched(const BatchInst *insts, const int64_t *row_off,
+                                           int ninst, int64_t total, cudaStream_t s);
+template <class T>
+cudaError_t launch_gather_jacobian_batched(const BatchInst *insts, const int64_t *blk_off,
+                                           int ninst, int64_t total, cudaStream_t s);
+template <class T>
+cudaError_t launch_gather_arclength_batched(const BatchInst *insts, const int64_t *row_off,
+                                            int ninst, int64_t total, cudaStream_t s);
+// occupancy of the persistent kernels (resident CTAs per SM)
+int exact_batched_ctas_per_sm(int elem_size, int form, int spec);
+int residual_batched_ctas_per_sm(int form);
 
 }  // namespace vefem

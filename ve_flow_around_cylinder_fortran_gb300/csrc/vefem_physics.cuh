@@ -22,13 +22,8 @@
 
 namespace vefem {
 
-enum { FORM_T = 0, FORM_SQRT = 1 };
-
-// Specialisations that leave out terms which are exact zeros for the given
-// parameters; a sum that drops an exact-zero addend keeps its value, so the
-// results are the same as the general code (up to the sign of a zero result).
-enum { SPEC_RE0 = 1,   // ReN == 0: convection, LSME-momentum and (ReN/dt, ReN*tsugn) terms
-       SPEC_DF0 = 2 }; // DfN == 0: stress diffusion terms and DfN/Helem^2
+// FORM_T / FORM_SQRT and the specialisations SPEC_RE0 / SPEC_DF0 are in
+// vefem_internal.h.
 enum { L_PTT = 0, M_L_PTT = 1, E_PTT = 2, M_E_PTT = 3, FENE_CR = 4, FENE_P = 5, GIESEKUS = 6 };
 
 // R is the scalar of state-dependent values, G the scalar of geometry values

@@ -7,7 +7,7 @@ This module adds a learned prediction in a reduced space:
 * POD: the converged snapshots x_1..x_m (state vector [TL, lambda]) are
   centred on their mean and decomposed by the method of snapshots (Gram
   matrix on the GPU, its eigenvectors on the host, modes re-orthonormalised
-  by QR); up to ``n_modes`` modes Phi with coefficients
+  by Cholesky QR); up to ``n_modes`` modes Phi with coefficients
   a_j = Phi^T (x_j - mean).
 * Network: the library's multilayer perceptron (vefem.MLP: 3 GELU layers of
   width 256, BF16 weights, FP32 accumulation, trained by the library's own
@@ -34,6 +34,8 @@ candidate only when its residual norm is below the tangent prediction's
 (ArclengthContinuation._judge).
 """
 from __future__ import annotations
+
+import time
 
 import numpy as np
 
@@ -62,6 +64,7 @@ class LearnedPredictor:
         self.coef = None     # [m][r] coefficients of the snapshots
         self.last_loss = None
         self.trainings = 0
+        self.timers = {"pod": 0.0, "train": 0.0, "predict": 0.0}
 
     # ---- data --------------------------------------------------------------
     def observe(self, k: int, x: np.ndarray, wi: float):
@@ -86,9 +89,13 @@ class LearnedPredictor:
         r = min(self.n_modes, int(keep.sum()))
         lam, V = lam[:r], V[:, :r]
         W = torch.from_numpy(V / np.sqrt(lam)).to(self.dev)
-        # re-orthonormalised: the snapshot method loses orthogonality in the
-        # weak modes by round-off ~ eps * lam_0 / lam_i
-        Phi = torch.linalg.qr(Xc @ W)[0]                      # N x r
+        # re-orthonormalised (two passes of Cholesky QR, the r x r factors on
+        # the host): the snapshot method loses orthogonality in the weak modes
+        # by round-off ~ eps * lam_0 / lam_i
+        Phi = Xc @ W                                          # N x r
+        for _ in range(2):
+            Lc = np.linalg.cholesky((Phi.T @ Phi).cpu().numpy())
+            Phi = Phi @ torch.from_numpy(np.linalg.inv(Lc).T.copy()).to(self.dev)
         if self.basis is not None:                            # keep mode signs stable
             old = self.basis[1]
             rr = min(r, old.shape[1])
@@ -121,9 +128,11 @@ class LearnedPredictor:
         return np.array(X), np.array(Y)
 
     def _fit(self):
+        t0 = time.perf_counter()
         mean, Phi, coef = self._pod()
         self.basis, self.coef = (mean, Phi), coef
         X, Y = self._dataset(coef)
+        t1 = time.perf_counter()
         xm, xs = X.mean(axis=0), X.std(axis=0)
         ym, ys = Y.mean(axis=0), Y.std(axis=0)
         xs = np.where(xs > 1e-12 * max(1.0, np.abs(xm).max()), xs, 1.0)
@@ -132,6 +141,8 @@ class LearnedPredictor:
         self.net.reset_optimizer()
         self.last_loss = self.net.train((X - xm) / xs, (Y - ym) / ys, self.iters, self.lr)
         self.trainings += 1
+        self.timers["pod"] += t1 - t0
+        self.timers["train"] += time.perf_counter() - t1
         if self.log:
             self.log(f"learned predictor: {len(self.X)} snapshots, {Phi.shape[1]} modes, "
                      f"training loss {self.last_loss:.3e}")
@@ -140,6 +151,7 @@ class LearnedPredictor:
     def predict(self, k: int, x_o: np.ndarray, t: np.ndarray, dS: float, x_plain: np.ndarray):
         if self.basis is None or len(self.X) < self.start:
             return None
+        t0 = time.perf_counter()
         torch = self.torch
         mean, Phi = self.basis
         m = len(self.X)
@@ -149,5 +161,6 @@ class LearnedPredictor:
         dy = self.net.forward(((f - xm) / xs)[None, :])[0].astype(np.float64) * ys + ym
         a = coef[m - 1] + dS * (quad + dy)
         r = Phi.shape[1]
-        cand = mean + Phi @ torch.from_numpy(a[:r]).to(self.dev)
-        return cand.cpu().numpy()
+        cand = (mean + Phi @ torch.from_numpy(a[:r]).to(self.dev)).cpu().numpy()
+        self.timers["predict"] += time.perf_counter() - t0
+        return cand

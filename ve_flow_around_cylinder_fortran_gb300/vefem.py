@@ -34,7 +34,11 @@ EXPORTED = ["vefem_abi_version", "vefem_create", "vefem_set_params", "vefem_asse
             "vefem_algorithmic_ops", "vefem_assemble_residual_noalloc",
             "vefem_mlp_create", "vefem_mlp_num_params", "vefem_mlp_set_params",
             "vefem_mlp_get_params", "vefem_mlp_forward", "vefem_mlp_loss_grad", "vefem_mlp_train",
-            "vefem_mlp_reset_optimizer", "vefem_mlp_destroy", "vefem_mlp_last_error"]
+            "vefem_mlp_reset_optimizer", "vefem_mlp_destroy", "vefem_mlp_last_error",
+            "vefem_batch_create", "vefem_batch_set_params", "vefem_assemble_batched",
+            "vefem_batch_autotune", "vefem_batch_set_tiles", "vefem_batch_info",
+            "vefem_batch_last_timing", "vefem_batch_destroy", "vefem_batch_last_error"]
+BATCH_CLASSES = 6
 
 
 class VefemError(RuntimeError):
@@ -96,6 +100,16 @@ def load(path: str = LIB_PATH):
     L.vefem_mlp_destroy.argtypes = [P]
     L.vefem_mlp_last_error.argtypes = [P]
     L.vefem_mlp_last_error.restype = ctypes.c_char_p
+    L.vefem_batch_create.argtypes = [I, P, P, P, ctypes.POINTER(P)]
+    L.vefem_batch_set_params.argtypes = [P, I, P]
+    L.vefem_assemble_batched.argtypes = [P, P, P, I, P, P, I]
+    L.vefem_batch_autotune.argtypes = [P, I, I, P]
+    L.vefem_batch_set_tiles.argtypes = [P, P]
+    L.vefem_batch_info.argtypes = [P, P]
+    L.vefem_batch_last_timing.argtypes = [P, P]
+    L.vefem_batch_destroy.argtypes = [P]
+    L.vefem_batch_last_error.argtypes = [P]
+    L.vefem_batch_last_error.restype = ctypes.c_char_p
     _lib = L
     return L
 
@@ -322,6 +336,102 @@ class MLP:
     def close(self):
         if getattr(self, "_h", None):
             self._L.vefem_mlp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class BatchAssembler:
+    """Batched form (vefem_batch_* in vefem.h): many instances -- meshes of
+    uneven size, each with its own parameters -- assembled together by one
+    persistent launch per kernel, replayed as a CUDA graph."""
+
+    def __init__(self, meshes, physs, patterns, device: int = 0):
+        L = load()
+        self._L = L
+        n = len(meshes)
+        if not (n == len(physs) == len(patterns)) or n == 0:
+            raise ValueError("meshes, physs and patterns must have the same non-zero length")
+        self.n = n
+        self._keep = []
+        cms = (c_mesh * n)()
+        ccs = (c_csr * n)()
+        cps = (c_params * n)()
+        self.N, self.nnz, self.nel, self.nnodes = [], [], [], []
+        for i, (m, p, (rp, ci)) in enumerate(zip(meshes, physs, patterns)):
+            conn = np.ascontiguousarray(m.conn, dtype=np.int32)
+            xyz = np.ascontiguousarray(m.xyz, dtype=np.float64)
+            rp = np.ascontiguousarray(rp, dtype=np.int64)
+            ci = np.ascontiguousarray(ci, dtype=np.int32)
+            self._keep += [conn, xyz, rp, ci]
+            cms[i] = c_mesh(int(m.nnodes), int(m.nel), conn.ctypes.data, xyz.ctypes.data, 0,
+                            None, None)
+            ccs[i] = c_csr(len(rp) - 1, rp.ctypes.data, ci.ctypes.data)
+            cps[i] = make_params(p, device)
+            self.N.append(len(rp) - 1)
+            self.nnz.append(len(ci))
+            self.nel.append(int(m.nel))
+            self.nnodes.append(int(m.nnodes))
+        h = ctypes.c_void_p()
+        rc = L.vefem_batch_create(n, cms, ccs, cps, ctypes.byref(h))
+        if rc:
+            raise VefemError(f"vefem_batch_create failed ({rc}): "
+                             f"{L.vefem_last_error(None).decode()}")
+        self._h = h
+        self.device = device
+
+    def _check(self, rc):
+        if rc:
+            raise VefemError(f"vefem batch error {rc}: "
+                             f"{self._L.vefem_batch_last_error(self._h).decode()}")
+
+    @staticmethod
+    def _parr(xs):
+        arr = (ctypes.c_void_p * len(xs))()
+        for i, x in enumerate(xs):
+            arr[i] = _ptr(x)
+        return arr
+
+    def set_params(self, i: int, phys):
+        p = make_params(phys, self.device)
+        self._check(self._L.vefem_batch_set_params(self._h, i, ctypes.byref(p)))
+
+    def assemble(self, TLs, EUs, flags: int, bs=None, valss=None, on_device: bool = False):
+        n = self.n
+        bs = bs if bs is not None else [None] * n
+        valss = valss if valss is not None else [None] * n
+        EUs = EUs if EUs is not None else [None] * n
+        self._check(self._L.vefem_assemble_batched(
+            self._h, self._parr(TLs), self._parr(EUs), flags, self._parr(bs), self._parr(valss),
+            1 if on_device else 0))
+
+    def autotune(self, flags: int, reps: int = 3):
+        t = (ctypes.c_int * BATCH_CLASSES)()
+        self._check(self._L.vefem_batch_autotune(self._h, flags, reps, t))
+        return list(t)
+
+    def set_tiles(self, tiles):
+        t = (ctypes.c_int * BATCH_CLASSES)(*tiles)
+        self._check(self._L.vefem_batch_set_tiles(self._h, t))
+
+    def info(self) -> dict:
+        o = (ctypes.c_int64 * 6)()
+        self._check(self._L.vefem_batch_info(self._h, o))
+        return {"instances": o[0], "elements": o[1], "work_items": o[2], "grid": o[3],
+                "launches": o[4], "replays": o[5]}
+
+    def last_timing(self):
+        t = (ctypes.c_float * 3)()
+        self._check(self._L.vefem_batch_last_timing(self._h, t))
+        return list(t)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.vefem_batch_destroy(self._h)
             self._h = None
 
     def __del__(self):
