@@ -5,7 +5,9 @@ Nex = 1 (the extra unknown lambda, Wi = Wi0 * lambda at every Gauss point):
 
 * continuationStepArclength (Continuation_Arclength_mod.F90:77-130): Newton
   at the predicted point, then direction, step control and the next
-  prediction;
+  prediction; each Newton solve starts in the mode checkMNR picks
+  (Newton_Raphson_mod.F90:72-78, 425-449), so a solve whose predecessor
+  started with a small correction reuses the previous factorisation;
 * the lambda equation (arclength, Extra_Equations_mod.F90:698-768): for the
   first two increments lambda is pinned, lambda - (LN0 + (k-1) dArN), with
   the lambda row and column replaced by the unit vector (MatZeroRowsColumns);
@@ -125,6 +127,8 @@ class ArclengthContinuation:
         self.N = asm.N
         self.nn = asm.nnodes
         self.judge_s = 0.0
+        self.cor0 = 1.0          # first correction norm of the last solve (cor_norm0_Main)
+        self.have_lu = False     # a factorisation exists (LS%maxit > 0)
 
     # state vector x = [TL in node-major order, lambda]
     def pack(self, TL, EU):
@@ -139,15 +143,26 @@ class ArclengthContinuation:
         rows, values = NW.boundary_conditions(self.mesh, p)
         self.dev.set_values(values)
 
-    def _newton(self, x0: np.ndarray, xF: float = 1.0, max_iter: int = NW.NITER):
-        """Newton with the lambda row and relaxation xF; returns (x, iterations,
-        factorisations, last residual norm, last LU, converged)."""
+    def _start_flag(self, k: int) -> str:
+        """checkMNR (Newton_Raphson_mod.F90:425-449): a solve starts with 'MNR'
+        -- the factorisation of the previous solve -- when the first correction
+        of the previous solve was below MNR_eps, except at every 100th
+        increment (if that correction was above MNR_eps/10) and every 1000th."""
+        flag = "MNR" if self.cor0 < NW.MNR_EPS else "NRP"
+        if (k % 100 == 0 and self.cor0 > NW.MNR_EPS / 10.0) or k % 1000 == 0:
+            flag = "NRP"
+        return flag if self.have_lu else "NRP"
+
+    def _newton(self, x0: np.ndarray, xF: float = 1.0, max_iter: int = NW.NITER,
+                flag: str = "NRP"):
+        """Newton with the lambda row and relaxation xF, starting in mode
+        ``flag``; returns (x, iterations, factorisations, last residual norm,
+        the solver holding the last factorisation, converged)."""
         cfg = self.cfg
         x = x0.copy()
         tm = self.timers
         res_norm = cor_new = cor_old = 1.0
-        flag = "NRP"
-        lu = None
+        lu = self.solver if self.have_lu else None
         it = nfac = 0
         while True:
             if cor_new < cfg.tol and res_norm < cfg.tol:
@@ -165,6 +180,7 @@ class ArclengthContinuation:
             t1 = time.perf_counter()
             if want:
                 lu = self.solver.factor(vals)
+                self.have_lu = True
                 nfac += 1
             t2 = time.perf_counter()
             s = lu.solve(b)
@@ -173,6 +189,8 @@ class ArclengthContinuation:
             tm["factor"] += t2 - t1
             tm["solve"] += t3 - t2
             cor_new = float(np.linalg.norm(s))
+            if it == 1:
+                self.cor0 = cor_new
             if self.log:
                 self.log(f"   {it:3d}. {flag}: RES_NORM = {res_norm:.4e}, COR_NORM = {cor_new:.4e}")
             if cor_new != cor_new or cor_new > NW.COR_NORM_DIV or it > max_iter:
@@ -215,8 +233,9 @@ class ArclengthContinuation:
             # from the prediction with the relaxation halved, 50 x Niter
             # iterations allowed and, on the arclength branch, dSo halved
             xF, max_it, its, nfac, emerg = 1.0, NW.NITER, 0, 0, 0
+            flag0 = self._start_flag(k)
             while True:
-                x, i1, f1, rn, lu, ok = self._newton(x_p, xF, max_it)
+                x, i1, f1, rn, lu, ok = self._newton(x_p, xF, max_it, flag0)
                 its += i1
                 nfac += f1
                 if ok:
@@ -227,6 +246,7 @@ class ArclengthContinuation:
                     raise RuntimeError(f"arclength Newton failed at increment {k} "
                                        f"(lambda = {x_p[-1]:.6g}, dS = {dS:.4g})")
                 max_it = 50 * NW.NITER
+                flag0 = "NRP"
                 if k > 2:
                     dS *= 0.5
                     self.lrow.dS = dS
