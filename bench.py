@@ -76,6 +76,8 @@ def parse_args():
                     help="run only the continuation comparison and print its JSON line")
     ap.add_argument("--batch-inst", type=int, default=64,
                     help="instances of the batched-form measurement (0 = skip it)")
+    ap.add_argument("--only", choices=["fd64", "residual", "exact64", "exact32"], default=None,
+                    help="time one assembly form alone on the --nel workload (profiling case)")
     return ap.parse_args()
 
 
@@ -252,12 +254,14 @@ def run_reference(args):
     return 0
 
 
-def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=None):
+def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=None,
+                         secant: bool = True):
     """Arclength continuation Wi 0.1 -> wi_end (Oldroyd-B, beta = 0.59, SQRT
-    form) on the GPU assembly, two arms from the same start: the plain FP64
-    path (FD64 Jacobian, tangent predictor) and the learned + mixed path
-    (FP32 exact Jacobian with FP64 residual, learned POD/MLP predictor trained
-    online after the first 20 points).  Every point is converged to
+    form) on the GPU assembly, arms from the same start: the plain FP64 path
+    (FD64 Jacobian, the reference's tangent predictor), the same with a
+    secant predictor, and the learned + mixed path (FP32 exact Jacobian with
+    FP64 residual, learned POD/MLP predictor trained online after the first
+    20 points).  Every point is converged to
     ||R|| < 1e-10 and ||dx|| < 1e-10; host wall time per arm."""
     from ve_flow_around_cylinder_fortran_gb300 import continuation as C
     from ve_flow_around_cylinder_fortran_gb300 import learned as LP
@@ -269,17 +273,25 @@ def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=Non
     asm = V.BulkAssembler(mesh, phys, rowptr, colind, outlet_edges=True, device=device)
     cfg = C.ArclengthSettings(dArN=0.01, lam_max=wi_end / phys.Wi0, max_steps=2000)
     arms, states = {}, {}
-    for name, jac, learned in (("plain_fp64", "fd64", False), ("learned_fp32", "exact32", True)):
+    runs = [("plain_fp64", "fd64", None), ("learned_fp32", "exact32", "learned")]
+    if secant:
+        runs.insert(1, ("secant_fp64", "fd64", "secant"))
+    for name, jac, kind in runs:
         cont = C.ArclengthContinuation(asm, mesh, phys, jac, cfg)
-        pred = LP.LearnedPredictor(n_modes=32, start=20, device=f"cuda:{device}") if learned else None
+        pred = None
+        if kind == "learned":
+            pred = LP.LearnedPredictor(n_modes=32, start=20, device=f"cuda:{device}")
+        elif kind == "secant":
+            pred = C.SecantPredictor()
         t0 = time.perf_counter()
         recs, xs = cont.run(TL, EU, predictor=pred)
         wall = time.perf_counter() - t0
-        if pred is not None:
+        if kind == "learned":
             pred.net.close()
         states[name] = xs
         arms[name] = {
-            "jacobian": jac, "predictor": "learned POD/MLP" if learned else "tangent",
+            "jacobian": jac,
+            "predictor": {"learned": "learned POD/MLP", "secant": "secant", None: "tangent"}[kind],
             "wall_s": wall, "steps": len(recs), "steps_per_s": len(recs) / wall,
             "newton_iterations": sum(r.newton_iterations for r in recs),
             "factorisations": sum(r.factorisations for r in recs),
@@ -292,7 +304,7 @@ def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=Non
                              "predictor": sum(r.predictor_s for r in recs)},
             "mean_dS_after_20": float(np.mean([r.dS for r in recs[20:]])) if len(recs) > 20 else None,
         }
-        if pred is not None:
+        if kind == "learned":
             arms[name]["predictor_split_s"] = dict(pred.timers, judge=cont.judge_s)
         if log:
             log(f"{name}: {arms[name]}")
@@ -389,6 +401,34 @@ def batched_compare(ninst: int, steps: int, warmup: int, device: int = 0, seed: 
     }
 
 
+def run_only(args, asm, mesh, TL, EU, cfg, dev):
+    """One assembly form alone, device-resident (the profiling case)."""
+    import torch
+    d = torch.device(f"cuda:{dev}")
+    jflag = {"fd64": V.VEFEM_JAC_FD64, "residual": 0, "exact64": V.VEFEM_JAC_EXACT64,
+             "exact32": V.VEFEM_JAC_EXACT32}[args.only]
+    flags = V.VEFEM_RESIDUAL | jflag | V.VEFEM_ZERO_FIRST
+    tTL = torch.from_numpy(TL).to(d)
+    tEU = torch.from_numpy(EU).to(d)
+    tb = torch.zeros(asm.N, dtype=torch.float64, device=d)
+    tv = None
+    if jflag:
+        tv = torch.zeros(asm.nnz, dtype=torch.float32 if args.only == "exact32" else torch.float64,
+                         device=d)
+    for _ in range(args.warmup):
+        asm.assemble(tTL, tEU, flags, tb, tv, on_device=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        asm.assemble(tTL, tEU, flags, tb, tv, on_device=True)
+    torch.cuda.synchronize()
+    s = time.perf_counter() - t0
+    print(json.dumps({"only": args.only, "value": mesh.nel * args.steps / s, "unit": UNIT,
+                      "steps": args.steps, "config": cfg}))
+    asm.close()
+    return 0
+
+
 def run_vefem(args):
     import torch
     world, rank, local, dist = dist_setup()
@@ -404,6 +444,8 @@ def run_vefem(args):
         return 0
     mesh, phys, TL, EU, rowptr, colind, cfg = workload(args.nel)
     asm = V.BulkAssembler(mesh, phys, rowptr, colind, device=dev)
+    if args.only:
+        return run_only(args, asm, mesh, TL, EU, cfg, dev)
     nel = mesh.nel
     d = torch.device(f"cuda:{dev}")
     tTL = torch.from_numpy(TL).to(d)
@@ -527,18 +569,12 @@ def run_vefem(args):
             "peak_source": "measured live: FP64 DFMA instruction rate of a probe kernel "
                            "(one instruction = one operation; this path cannot use FMA)",
             "dadd_peak": peaks["dadd_inst_per_s"] / 1e12, "dmul_peak": peaks["dmul_inst_per_s"] / 1e12}
-    cpu = None
-    if world == 1 and not args.no_cpu_baseline:
-        rate, n, cores, times = cpu_oracle_rate(phys, mesh, TL, EU, rowptr, colind, 6.0, 3)
-        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"first {n} of {nel} elements, residual + FD Jacobian into AIJ, "
-                         f"median of 3 ({', '.join(f'{x:.2f}' for x in times)} s)"}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": cfg, "e2e": e2e, "gpu_launches": launches, "roofline": roof,
-        "cpu_baseline": cpu, "clocks": clk,
+        "cpu_baseline": None, "clocks": clk,
         "residual_only": {"value": nel * args.steps / (r_ms * 1e-3), "unit": UNIT,
                           "kernel_ms_avg": statistics.mean(r_k)},
     }
@@ -548,6 +584,14 @@ def run_vefem(args):
         line["batched"] = batched_compare(args.batch_inst, max(3, args.steps // 2), args.warmup, dev)
     if world == 1 and args.cont_nel > 0:
         line["continuation"] = continuation_compare(args.cont_nel, args.cont_wi, dev)
+    # the CPU baseline runs last: its OpenMP worker threads stay on the host
+    # cores afterwards and would slow the host side of the parts above
+    if world == 1 and not args.no_cpu_baseline:
+        rate, n, cores, times = cpu_oracle_rate(phys, mesh, TL, EU, rowptr, colind, 6.0, 3)
+        line["cpu_baseline"] = {
+            "value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"first {n} of {nel} elements, residual + FD Jacobian into AIJ, "
+                      f"median of 3 ({', '.join(f'{x:.2f}' for x in times)} s)"}
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()

@@ -19,8 +19,10 @@ _lib = None
 
 
 def build(force: bool = False) -> str:
-    if force or not os.path.exists(SO) or os.path.getmtime(SO) < os.path.getmtime(
-            os.path.join(HERE, "vefem_oracle.c")):
+    srcs = [os.path.join(HERE, f) for f in ("vefem_oracle.c", "vefem_stability_oracle.c",
+                                           "build.sh")]
+    if force or not os.path.exists(SO) or any(os.path.getmtime(SO) < os.path.getmtime(f)
+                                              for f in srcs):
         subprocess.check_call(["bash", os.path.join(HERE, "build.sh")])
     return SO
 
@@ -37,6 +39,9 @@ def lib():
         L.ora_edge_open.argtypes = [P, P, I, I, P, P, P, P, I, I, P, P, P]
         L.ora_gp_probe.argtypes = [P, P, I, I, P, P, P, P, I, P]
         L.ora_gauss_tables.argtypes = [P, P]
+        D = ctypes.c_double
+        L.ora_stability_batch.argtypes = [P, P, D, I, I, I, P, P, P, P, I, I, P, P, P, P, I]
+        L.ora_stability_batch.restype = I
         for f in (L.ora_element_batch, L.ora_assemble, L.ora_edge_open, L.ora_gp_probe):
             f.restype = I
         _lib = L
@@ -117,3 +122,30 @@ def gp_probe(phys, conn, xyz, TL, EU, iel):
     lib().ora_gp_probe(_p(ip), _p(dp), conn.shape[1], xyz.shape[1], _p(conn), _p(xyz), _p(TL),
                        _p(EU), int(iel), _p(out))
     return out
+
+
+def stability_elements(phys, conn, xyz, TLb, TLd, KwN: float, kz: bool = True, jacobian=True,
+                       e0: int = 0, e1: int | None = None, nthreads: int = 0):
+    """Stability element outputs (vefem_stability_oracle.c): Res_a, Res_b
+    [nel][9][10] and the FD blocks A, B [nel][9][10][9][10] (inod, ieq, jnod, jeq)."""
+    L = lib()
+    ip = np.ascontiguousarray(phys.int_params(), dtype=np.int32)
+    dp = np.ascontiguousarray(phys.dbl_params(), dtype=np.float64)
+    conn = np.ascontiguousarray(conn, dtype=np.int32)
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    TLb = np.ascontiguousarray(TLb, dtype=np.float64)
+    TLd = np.ascontiguousarray(TLd, dtype=np.float64)
+    nel = conn.shape[1]
+    nnodes = TLb.shape[1]
+    e1 = nel if e1 is None else e1
+    n = e1 - e0
+    ra = np.zeros((n, 9, 10))
+    rb = np.zeros((n, 9, 10))
+    A = np.zeros((n, 9, 10, 9, 10)) if jacobian else None
+    B = np.zeros((n, 9, 10, 9, 10)) if jacobian else None
+    rc = L.ora_stability_batch(_p(ip), _p(dp), float(KwN), 1 if kz else 0, nel, nnodes, _p(conn),
+                               _p(xyz), _p(TLb), _p(TLd), e0, e1, _p(ra), _p(rb), _p(A), _p(B),
+                               nthreads)
+    if rc:
+        raise ValueError(f"ora_stability_batch: {rc} (T form and non-FENE models only)")
+    return ra, rb, A, B

@@ -106,6 +106,27 @@ class LambdaRow:
                 vals[r0:r1] = self.t
 
 
+class SecantPredictor:
+    """Secant prediction x_p = x_k + dS (x_k - x_{k-1}) / |x_k - x_{k-1}| in
+    place of the reference's tangent (the reference uses the secant only at
+    increment 2, setDirectionVectors, Continuation_Arclength_mod.F90:183-206).
+    It replaces the tangent step outright (no residual judging)."""
+
+    replaces = True
+
+    def __init__(self):
+        self.last = []
+
+    def observe(self, k, x, wi):
+        self.last = (self.last + [x.copy()])[-2:]
+
+    def predict(self, k, x_o, t, dS, x_plain):
+        if len(self.last) < 2:
+            return None
+        d = self.last[1] - self.last[0]
+        return self.last[1] + d * (dS / np.linalg.norm(d))
+
+
 class ArclengthContinuation:
     """loopArclength for one mesh and one assembler (nex = 1)."""
 
@@ -226,7 +247,9 @@ class ArclengthContinuation:
             if predictor is not None and k > 2:
                 tp = time.perf_counter()
                 cand = predictor.predict(k, x_o, t, dS, x_p)
-                if cand is not None:
+                if cand is not None and getattr(predictor, "replaces", False):
+                    x_p, pred_name = cand, type(predictor).__name__
+                elif cand is not None:
                     x_p, pred_name = self._judge(x_p, cand)
                 self.timers["predictor"] += time.perf_counter() - tp
             # emergencyNewtonRaphson (Newton_Raphson_mod.F90:533-584): restart

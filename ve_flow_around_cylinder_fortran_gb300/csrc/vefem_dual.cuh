@@ -6,6 +6,10 @@
 
 #include <math.h>
 
+#include <type_traits>
+
+#include "vefem_scalar.cuh"
+
 #ifdef __CUDACC__
 #define VD_HD __host__ __device__ __forceinline__
 #else
@@ -31,6 +35,11 @@ struct Dual {
     VD_HD Dual(T x, T dx) : v(x), d(dx) {}
 };
 
+template <class T>
+struct ScalarOf<Dual<T>> {
+    typedef T type;
+};
+
 template <class T> VD_HD Dual<T> operator+(Dual<T> a, Dual<T> b) { return Dual<T>(a.v + b.v, a.d + b.d); }
 template <class T> VD_HD Dual<T> operator-(Dual<T> a, Dual<T> b) { return Dual<T>(a.v - b.v, a.d - b.d); }
 template <class T> VD_HD Dual<T> operator*(Dual<T> a, Dual<T> b)
@@ -44,18 +53,22 @@ template <class T> VD_HD Dual<T> operator/(Dual<T> a, Dual<T> b)
 }
 template <class T> VD_HD Dual<T> operator-(Dual<T> a) { return Dual<T>(-a.v, -a.d); }
 
-template <class T> VD_HD Dual<T> operator+(Dual<T> a, double b) { return Dual<T>(a.v + (T)b, a.d); }
-template <class T> VD_HD Dual<T> operator-(Dual<T> a, double b) { return Dual<T>(a.v - (T)b, a.d); }
-template <class T> VD_HD Dual<T> operator*(Dual<T> a, double b) { return Dual<T>(a.v * (T)b, a.d * (T)b); }
-template <class T> VD_HD Dual<T> operator/(Dual<T> a, double b) { return Dual<T>(a.v / (T)b, a.d / (T)b); }
-template <class T> VD_HD Dual<T> operator+(double a, Dual<T> b) { return Dual<T>((T)a + b.v, b.d); }
-template <class T> VD_HD Dual<T> operator-(double a, Dual<T> b) { return Dual<T>((T)a - b.v, -b.d); }
-template <class T> VD_HD Dual<T> operator*(double a, Dual<T> b) { return Dual<T>((T)a * b.v, (T)a * b.d); }
-template <class T> VD_HD Dual<T> operator/(double a, Dual<T> b)
+// Dual (op) scalar: the scalar is converted to T once (a float path never
+// widens to FP64, whose pipe is narrow on this GPU; literals fold)
+#define VD_SCALAR template <class T, class U, typename std::enable_if<std::is_arithmetic<U>::value, int>::type = 0>
+VD_SCALAR VD_HD Dual<T> operator+(Dual<T> a, U b) { return Dual<T>(a.v + (T)b, a.d); }
+VD_SCALAR VD_HD Dual<T> operator-(Dual<T> a, U b) { return Dual<T>(a.v - (T)b, a.d); }
+VD_SCALAR VD_HD Dual<T> operator*(Dual<T> a, U b) { return Dual<T>(a.v * (T)b, a.d * (T)b); }
+VD_SCALAR VD_HD Dual<T> operator/(Dual<T> a, U b) { return Dual<T>(a.v / (T)b, a.d / (T)b); }
+VD_SCALAR VD_HD Dual<T> operator+(U a, Dual<T> b) { return Dual<T>((T)a + b.v, b.d); }
+VD_SCALAR VD_HD Dual<T> operator-(U a, Dual<T> b) { return Dual<T>((T)a - b.v, -b.d); }
+VD_SCALAR VD_HD Dual<T> operator*(U a, Dual<T> b) { return Dual<T>((T)a * b.v, (T)a * b.d); }
+VD_SCALAR VD_HD Dual<T> operator/(U a, Dual<T> b)
 {
     const T q = (T)a / b.v;
     return Dual<T>(q, -q * b.d / b.v);
 }
+#undef VD_SCALAR
 
 template <class T> VD_HD Dual<T> sqrt(Dual<T> a)
 {

@@ -39,6 +39,14 @@ __constant__ double x_dfde[9][9];
 __constant__ double x_d2fdc2[9][9];
 __constant__ double x_d2fde2[9][9];
 __constant__ double x_d2fdce[9][9];
+// FP32 copies for the FP32 Jacobian (its geometry runs in FP32 on coordinates
+// relative to the element's first node)
+__constant__ float xf_w[9];
+__constant__ float xf_dfdc[9][9];
+__constant__ float xf_dfde[9][9];
+__constant__ float xf_d2fdc2[9][9];
+__constant__ float xf_d2fde2[9][9];
+__constant__ float xf_d2fdce[9][9];
 
 cudaError_t upload_tables_exact(const GaussTables &t, cudaStream_t s)
 {
@@ -54,11 +62,32 @@ cudaError_t upload_tables_exact(const GaussTables &t, cudaStream_t s)
     UP(x_d2fde2, t.d2fde2)
     UP(x_d2fdce, t.d2fdce)
 #undef UP
+    float w[9], a[5][9][9];
+    for (int i = 0; i < 9; i++) {
+        w[i] = (float)t.w[i];
+        for (int j = 0; j < 9; j++) {
+            a[0][i][j] = (float)t.dfdc[i][j];
+            a[1][i][j] = (float)t.dfde[i][j];
+            a[2][i][j] = (float)t.d2fdc2[i][j];
+            a[3][i][j] = (float)t.d2fde2[i][j];
+            a[4][i][j] = (float)t.d2fdce[i][j];
+        }
+    }
+    if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(xf_w, w, sizeof(w), 0, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(xf_dfdc, a[0], sizeof(a[0]), 0, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(xf_dfde, a[1], sizeof(a[1]), 0, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(xf_d2fdc2, a[2], sizeof(a[2]), 0, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(xf_d2fde2, a[3], sizeof(a[3]), 0, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(xf_d2fdce, a[4], sizeof(a[4]), 0, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);   // the host staging arrays go out of scope
     return e;
 }
 
 constexpr int EX_THREADS = 192;
 constexpr int EX_NDIR = 21;      // 20 interpolated quantities + the arclength unknown
+// row stride of A: 54 entries padded to 58, which cuts the shared-memory bank
+// conflicts of the contraction's reads (qdir(f, s) rows at once) by a third
+constexpr int EX_AST = 58;
 
 // direction index of quantity s (0 value, 1 d/dx, 2 d/dy, 3 Laplacian) of field f
 __device__ __forceinline__ int qdir(int f, int s)
@@ -78,36 +107,47 @@ __device__ __forceinline__ void exact_element(const ElemArgs &a, const KParams &
 {
     extern __shared__ __align__(16) unsigned char smraw[];
     T *D = reinterpret_cast<T *>(smraw);               // [9][21][18]
-    T *A = D + 9 * EX_NDIR * 18;                       // [9][21][54]
+    T *A = D + 9 * EX_NDIR * 18;                       // [9][21][EX_AST]
     __shared__ T s_tl[54];
     __shared__ T s_dFx[9][9], s_dFy[9][9], s_d2x[9][9], s_d2y[9][9], s_lap[9][9];
     __shared__ T s_H2[9], s_WET[9];
+    __shared__ T s_bfn[9][9];          // basis values in T: no FP64 conversions in the loops
     const int t = threadIdx.x;
+    if (t >= 96 && t < 96 + 81) s_bfn[(t - 96) / 9][(t - 96) % 9] = (T)x_bfn[(t - 96) / 9][(t - 96) % 9];
 
     if (t < 54) {
         const int inod = t / 6, f = t - 6 * (t / 6);
         s_tl[t] = (T)a.TL[(size_t)f * a.nnodes + a.conn[inod * a.nel + e]];
     } else if (t >= 64 && t < 73) {
         const int ig = t - 64;
-        double x[9], y[9], fx[9], fy[9], sx[9], sy[9];
+        // coordinates relative to node 0 (the map's derivatives see only
+        // differences), then the geometry in T
+        T x[9], y[9], fx[9], fy[9], sx[9], sy[9];
+        const int g0 = a.conn[e];
+        const double x0 = a.xy[g0], y0 = a.xy[a.nnodes + g0];
 #pragma unroll
         for (int n = 0; n < 9; n++) {
             const int gn = a.conn[n * a.nel + e];
-            x[n] = a.xy[gn];
-            y[n] = a.xy[a.nnodes + gn];
+            x[n] = (T)(a.xy[gn] - x0);
+            y[n] = (T)(a.xy[a.nnodes + gn] - y0);
         }
-        auto go = geometry(x_bfn[ig], x_dfdc[ig], x_dfde[ig], x_d2fdc2[ig], x_d2fde2[ig],
-                           x_d2fdce[ig], x_w[ig], x, y, fx, fy, sx, sy);
+        GeoOut<T> go;
+        if constexpr (sizeof(T) == 4)
+            go = geometry(xf_dfdc[ig], xf_dfdc[ig], xf_dfde[ig], xf_d2fdc2[ig], xf_d2fde2[ig],
+                          xf_d2fdce[ig], xf_w[ig], x, y, fx, fy, sx, sy);
+        else
+            go = geometry(x_dfdc[ig], x_dfdc[ig], x_dfde[ig], x_d2fdc2[ig], x_d2fde2[ig],
+                          x_d2fdce[ig], x_w[ig], x, y, fx, fy, sx, sy);
 #pragma unroll
         for (int n = 0; n < 9; n++) {
-            s_dFx[ig][n] = (T)fx[n];
-            s_dFy[ig][n] = (T)fy[n];
-            s_d2x[ig][n] = (T)sx[n];
-            s_d2y[ig][n] = (T)sy[n];
-            s_lap[ig][n] = (T)(sx[n] + sy[n]);
+            s_dFx[ig][n] = fx[n];
+            s_dFy[ig][n] = fy[n];
+            s_d2x[ig][n] = sx[n];
+            s_d2y[ig][n] = sy[n];
+            s_lap[ig][n] = sx[n] + sy[n];
         }
-        s_H2[ig] = (T)go.H2;
-        s_WET[ig] = (T)go.WET;
+        s_H2[ig] = go.H2;
+        s_WET[ig] = go.WET;
     }
     __syncthreads();
 
@@ -117,7 +157,7 @@ __device__ __forceinline__ void exact_element(const ElemArgs &a, const KParams &
         if (d < 20 || prm.nex > 0) {
             typedef Dual<T> R;
             TView<T> V{s_tl};
-            const Interp<T> Ip = interpolate(V, x_bfn[gp], s_dFx[gp], s_dFy[gp], s_d2x[gp],
+            const Interp<T> Ip = interpolate(V, s_bfn[gp], s_dFx[gp], s_dFy[gp], s_d2x[gp],
                                              s_d2y[gp]);
             Interp<R> I;
 #define SEED(field, idx) I.field = R(Ip.field, d == (idx) ? (T)1 : (T)0)
@@ -141,7 +181,7 @@ __device__ __forceinline__ void exact_element(const ElemArgs &a, const KParams &
             for (int k = 0; k < 3; k++) {
                 R o[6];
                 const R du = k == 0 ? R(0.0) : (k == 1 ? g.U1 : g.U2);
-                test_node<FORM, SPEC>(g, prm, k == 0 ? 1.0 : 0.0, (T)(k == 1 ? 1 : 0),
+                test_node<FORM, SPEC>(g, prm, (T)(k == 0 ? 1 : 0), (T)(k == 1 ? 1 : 0),
                                       (T)(k == 2 ? 1 : 0), du, (T)1, o);
 #pragma unroll
                 for (int q = 0; q < 6; q++) dst[q * 3 + k] = o[q].d;
@@ -156,8 +196,8 @@ __device__ __forceinline__ void exact_element(const ElemArgs &a, const KParams &
         const int gd = it / 9;               // gp*21 + d
         const int gp = gd / EX_NDIR;
         const T *dd = D + gd * 18;
-        const T b0 = (T)x_bfn[gp][i], b1 = s_dFx[gp][i], b2 = s_dFy[gp][i], w = s_WET[gp];
-        T *dst = A + gd * 54 + i * 6;
+        const T b0 = s_bfn[gp][i], b1 = s_dFx[gp][i], b2 = s_dFy[gp][i], w = s_WET[gp];
+        T *dst = A + gd * EX_AST + i * 6;
 #pragma unroll
         for (int q = 0; q < 6; q++)
             dst[q] = w * (b0 * dd[q * 3 + 0] + b1 * dd[q * 3 + 1] + b2 * dd[q * 3 + 2]);
@@ -173,18 +213,18 @@ __device__ __forceinline__ void exact_element(const ElemArgs &a, const KParams &
         const int ns = f < 2 ? 4 : 3;
         T acc = 0;
         for (int gp = 0; gp < 9; gp++) {
-            const T *ag = A + gp * EX_NDIR * 54 + i * 6 + q;
+            const T *ag = A + gp * EX_NDIR * EX_AST + i * 6 + q;
             const int q0 = qdir(f, 0);
-            acc += ag[q0 * 54] * (T)x_bfn[gp][j];
-            acc += ag[(q0 + 1) * 54] * s_dFx[gp][j];
-            acc += ag[(q0 + 2) * 54] * s_dFy[gp][j];
-            if (ns == 4) acc += ag[(q0 + 3) * 54] * s_lap[gp][j];
+            acc += ag[q0 * EX_AST] * s_bfn[gp][j];
+            acc += ag[(q0 + 1) * EX_AST] * s_dFx[gp][j];
+            acc += ag[(q0 + 2) * EX_AST] * s_dFy[gp][j];
+            if (ns == 4) acc += ag[(q0 + 3) * EX_AST] * s_lap[gp][j];
         }
         out[o] = acc;
     }
     if (prm.nex > 0 && t < 54) {
         T acc = 0;
-        for (int gp = 0; gp < 9; gp++) acc += A[(gp * EX_NDIR + 20) * 54 + t];
+        for (int gp = 0; gp < 9; gp++) acc += A[(gp * EX_NDIR + 20) * EX_AST + t];
         as[(size_t)e * 54 + t] = acc;
     }
 }
@@ -192,7 +232,7 @@ __device__ __forceinline__ void exact_element(const ElemArgs &a, const KParams &
 // persistent form over the work items of many meshes; each item is a run of
 // consecutive elements of one mesh (the element-batch tile of its size class)
 template <class T, int FORM, int SPEC>
-__global__ void __launch_bounds__(EX_THREADS)
+__global__ void __launch_bounds__(EX_THREADS, sizeof(T) == 4 ? 3 : 1)
 k_exact_batched(const BatchInst *__restrict__ insts, const WorkItem *__restrict__ work, int nwork)
 {
     for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
@@ -213,7 +253,7 @@ template <class T, int FORM, int SPEC>
 static cudaError_t go_exact_batched(const BatchInst *insts, const WorkItem *work, int nwork,
                                     int grid, cudaStream_t s)
 {
-    const size_t smem = sizeof(T) * (9 * EX_NDIR * 18 + 9 * EX_NDIR * 54);
+    const size_t smem = sizeof(T) * (9 * EX_NDIR * 18 + 9 * EX_NDIR * EX_AST);
     cudaError_t e = cudaFuncSetAttribute(k_exact_batched<T, FORM, SPEC>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -237,7 +277,7 @@ cudaError_t launch_exact_batched(const BatchInst *insts, const WorkItem *work, i
 template <class T, int FORM, int SPEC>
 static int occ_exact()
 {
-    const size_t smem = sizeof(T) * (9 * EX_NDIR * 18 + 9 * EX_NDIR * 54);
+    const size_t smem = sizeof(T) * (9 * EX_NDIR * 18 + 9 * EX_NDIR * EX_AST);
     if (cudaFuncSetAttribute(k_exact_batched<T, FORM, SPEC>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return 0;

@@ -42,6 +42,19 @@ inline Cd sqrt(Cd a) { g_tally->sqrt++; return Cd(::sqrt(a.v)); }
 inline Cd exp(Cd a) { g_tally->exp++; return Cd(::exp(a.v)); }
 inline Cd fabs(Cd a) { return Cd(::fabs(a.v)); }
 
+}  // namespace
+
+// parameters stay plain doubles when counting: their conversions and the
+// arithmetic on parameters alone are per-launch constants, not element work
+namespace vefem {
+template <>
+struct ScalarOf<Cd> {
+    typedef double type;
+};
+}  // namespace vefem
+
+namespace {
+
 struct ArrView {
     const Cd *p;
     Cd operator()(int pos) const { return p[pos]; }

@@ -13,6 +13,7 @@
 #include <math.h>
 
 #include "vefem_internal.h"
+#include "vefem_scalar.cuh"
 
 #ifdef __CUDACC__
 #define VF_HD __host__ __device__ __forceinline__
@@ -39,10 +40,10 @@ struct GeoOut {
     R H2, WET, detJ;
 };
 
-template <class R>
-VF_HD GeoOut<R> geometry(const double *bfn_unused, const double *dfdc, const double *dfde,
-                        const double *d2c, const double *d2e, const double *d2ce, double w,
-                        const R *x, const R *y, R *dFx, R *dFy, R *d2x, R *d2y)
+template <class R, class B>
+VF_HD GeoOut<R> geometry(const B *bfn_unused, const B *dfdc, const B *dfde, const B *d2c,
+                        const B *d2e, const B *d2ce, B w, const R *x, const R *y, R *dFx,
+                        R *dFy, R *d2x, R *d2y)
 {
     (void)bfn_unused;
     R dxdc = 0.0, dydc = 0.0, dxde = 0.0, dyde = 0.0;
@@ -66,11 +67,11 @@ VF_HD GeoOut<R> geometry(const double *bfn_unused, const double *dfdc, const dou
         const R fy = (dcdy * dfdc[n] + dedy * dfde[n]);
         dFx[n] = fx;
         dFy[n] = fy;
-        d2x[n] = (dcdx * dcdx) * d2c[n] + (dedx * dedx) * d2e[n] + 2.0 * dcdx * dedx * d2ce[n];
-        d2y[n] = (dcdy * dcdy) * d2c[n] + (dedy * dedy) * d2e[n] + 2.0 * dcdy * dedy * d2ce[n];
+        d2x[n] = (dcdx * dcdx) * d2c[n] + (dedx * dedx) * d2e[n] + (R)2.0 * dcdx * dedx * d2ce[n];
+        d2y[n] = (dcdy * dcdy) * d2c[n] + (dedy * dedy) * d2e[n] + (R)2.0 * dcdy * dedy * d2ce[n];
         hs = hs + fx * fx + fy * fy;
     }
-    const R helem = 1.0 / sqrt(hs);
+    const R helem = (R)1.0 / sqrt(hs);
     g.H2 = helem * helem;
     g.WET = w * fabs(g.detJ);
     return g;
@@ -100,8 +101,8 @@ struct GpCoef {
 };
 
 // interpolation from a state accessor V(pos), pos = inod*6 + ieq
-template <class R, class View>
-VF_HD Interp<R> interpolate(const View &V, const double *bfn, const R *dFx, const R *dFy,
+template <class R, class View, class B>
+VF_HD Interp<R> interpolate(const View &V, const B *bfn, const R *dFx, const R *dFy,
                             const R *d2x, const R *d2y)
 {
     Interp<R> I;
@@ -197,9 +198,10 @@ template <int FORM, int SPEC = 0, class R, class G>
 VF_HD GpCoef<R> gauss_point(const Interp<R> &I, const KParams &prm, R WiN, G H2, const G *dFx,
                             const G *dFy, R *dotU)
 {
+    typedef typename ScalarOf<R>::type S;
     GpCoef<R> g;
-    const double BvN = prm.BvN, ReN = prm.ReN, VeN = prm.VeN, DfN = prm.DfN;
-    const double omb = 1.0 - BvN;
+    const S BvN = (S)prm.BvN, ReN = (S)prm.ReN, VeN = (S)prm.VeN, DfN = (S)prm.DfN;
+    const S omb = (S)1.0 - BvN;
     g.omb = omb;
     g.WiN = WiN;
     g.U1 = I.U1;
@@ -228,7 +230,7 @@ VF_HD GpCoef<R> gauss_point(const Interp<R> &I, const KParams &prm, R WiN, G H2,
         if (prm.model == FENE_CR || prm.model == FENE_P) {
             // setFENEMaterialDerivative :272-311 (steady)
             const R dfx0 = I.dS11x + I.dS22x, dfy0 = I.dS11y + I.dS22y;
-            const double den = (prm.model == FENE_P) ? VeN : (VeN - 2.0);
+            const S den = (prm.model == FENE_P) ? VeN : (VeN - (S)2.0);
             const R dfx = (WiN / omb) * dfx0 / den;
             const R dfy = (WiN / omb) * dfy0 / den;
             MDfDt = I.U1 * dfx + I.U2 * dfy;
@@ -418,7 +420,7 @@ VF_HD GpCoef<R> gauss_point(const Interp<R> &I, const KParams &prm, R WiN, G H2,
     if (SPEC & SPEC_RE0) {
         tlsme = a3 * a3 + a4 * a4;
     } else {
-        const R a1 = ReN / prm.dt, a2 = ReN * tsugn;
+        const R a1 = ReN / (S)prm.dt, a2 = ReN * tsugn;
         tlsme = a1 * a1 + a2 * a2 + a3 * a3 + a4 * a4;
     }
     tlsme = 1.0 / sqrt(tlsme);
@@ -428,12 +430,12 @@ VF_HD GpCoef<R> gauss_point(const Interp<R> &I, const KParams &prm, R WiN, G H2,
     R tdcs = 0.5 * ddS;
     if (FORM == FORM_T) tdcs = tdcs + r * r;
     tdcs = H2 / sqrt(tdcs);
-    if (DfN > 1.0e-12) tdcs = 0.0;
+    if (DfN > (S)1.0e-12) tdcs = 0.0;
     g.tdcs = tdcs;
     R mag = (((C11 * C11 + C12 * C21) + C21 * C12) + C22 * C22) + C33 * C33;
     mag = sqrt(0.5 * mag);
     g.mag = mag;
-    const R b1 = WiN / prm.dt, b2 = WiN * tsugn, b3 = WiN * sqrt(0.5 * ddG), b4 = f2;
+    const R b1 = WiN / (S)prm.dt, b2 = WiN * tsugn, b3 = WiN * sqrt(0.5 * ddG), b4 = f2;
     const R b5 = f3 * sqrt(0.5 * ddC), b6 = tdcs * mag / H2;
     R tlsce = b1 * b1 + b2 * b2 + b3 * b3 + b4 * b4 + b5 * b5 + b6 * b6;
     if (!(SPEC & SPEC_DF0)) {
@@ -448,11 +450,12 @@ VF_HD GpCoef<R> gauss_point(const Interp<R> &I, const KParams &prm, R WiN, G H2,
 
 // Weak-form terms of one test node n (momentumMain(SQRT), continuityBulkMain,
 // stressesBulkMain(SQRT), Residuals_mod.F90:44-157, 295-490) times WET.
-template <int FORM, int SPEC = 0, class R, class G, class Out>
-VF_HD void test_node(const GpCoef<R> &g, const KParams &prm, double bifn, G fx, G fy, R du,
+template <int FORM, int SPEC = 0, class R, class B, class G, class Out>
+VF_HD void test_node(const GpCoef<R> &g, const KParams &prm, B bifn, G fx, G fy, R du,
                      G WET, Out *out)
 {
-    const R DfN = prm.DfN;
+    typedef typename ScalarOf<R>::type S;
+    const R DfN = (S)prm.DfN;
     // momentum
     R lsme1, lsme2;
     if (!(SPEC & SPEC_RE0)) {

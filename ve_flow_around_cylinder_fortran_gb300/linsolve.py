@@ -10,9 +10,9 @@ come last.  On the cylinder meshes this factorises about 4x faster with
 about half the fill of SuperLU's column-AMD order.
 
 The factorisation takes diagonal pivots (diag_pivot_thresh 0, the order is
-fixed by the dissection); when the relative residual of a solve exceeds
-``check_tol`` the matrix is refactorised with threshold partial pivoting
-and the solve repeated.
+fixed by the dissection); when a pivot is exactly zero, or the relative
+residual of a solve exceeds ``check_tol``, the matrix is refactorised with
+partial pivoting (and the solve repeated).
 """
 from __future__ import annotations
 
@@ -85,11 +85,16 @@ class SparseLU:
         if self.perm is not None:
             A = A[self.perm][:, self.perm]
         self.A = A.tocsc()
-        if self.perm is not None:
-            self.lu = spla.splu(self.A, permc_spec="NATURAL", diag_pivot_thresh=0.0)
-        else:
-            self.lu = spla.splu(self.A, permc_spec="COLAMD")
         self.pivoted = self.perm is None
+        if self.perm is None:
+            self.lu = spla.splu(self.A, permc_spec="COLAMD")
+            return self
+        try:
+            self.lu = spla.splu(self.A, permc_spec="NATURAL", diag_pivot_thresh=0.0)
+        except RuntimeError:        # an exactly zero diagonal pivot
+            self.lu = spla.splu(self.A, permc_spec="NATURAL", diag_pivot_thresh=1.0)
+            self.pivoted = True
+            self.refactorisations += 1
         return self
 
     def solve(self, b: np.ndarray) -> np.ndarray:
