@@ -197,6 +197,28 @@ int vefem_assemble_residual_noalloc(const vefem_params *params, int nnodes, int 
 
 int vefem_abi_version(void);
 
+/* ---- Linear stability: batched A/B assembly --------------------------------
+ * setEquationsBulkStability (Stability/Equations_Stability_mod.F90:20-226):
+ * the matrices of the generalised eigenproblem A x = lambda B x for
+ * spanwise-periodic 3-D perturbations of the steady 2-D state, 10 unknowns
+ * per node (Ux, Uy, Uz, P, Txx, Txy, Tyy, Txz, Tyz, Tzz), node-major rows.
+ * TLb [10][nnodes] is the base embedded as updateStabilityArrays does
+ * (Continuation_Stability_mod.F90:592-633: [Ux, Uy, 0, P, Txx, Txy, Tyy, 0, 0, 0]);
+ * Wi is params.WiN.  A[k] receives A at wavenumber kw[k] (k = 0..nk-1) and B
+ * the k-independent B, ADD semantics, on the pattern vefem_stability_pattern
+ * returns (query sizes with rowptr = colind = NULL first).  T form and the
+ * L-PTT, m-L-PTT, e-PTT, m-e-PTT and Giesekus models; Dirichlet rows are the
+ * caller's (applyDirichletBCStability: A row -> unit row, B row -> 0).
+ * The reference comments out the z-derivatives of the perturbation
+ * (Element_Calculations_Stability_mod.F90:52-79); they are included unless
+ * VEFEM_STAB_AS_WRITTEN is given. */
+#define VEFEM_STAB_AS_WRITTEN 0x2000
+
+int vefem_stability_pattern(vefem_ctx *ctx, int64_t *n, int64_t *nnz, int64_t *rowptr,
+                            int32_t *colind);
+int vefem_stability_assemble(vefem_ctx *ctx, const double *TLb, int nk, const double *kw,
+                             int flags, double *const *A, double *B, int on_device);
+
 /* ---- Batched form ---------------------------------------------------------
  * Many independent instances (Weissenberg points, meshes of uneven size)
  * assembled by one persistent launch per kernel, replayed as a CUDA graph.

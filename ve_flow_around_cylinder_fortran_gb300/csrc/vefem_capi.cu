@@ -724,7 +724,8 @@ extern "C" int vefem_destroy(vefem_ctx *ctx)
                     ctx->d_edge_row, ctx->d_edge_off, ctx->d_rs, ctx->d_es, ctx->d_as,
                     ctx->d_ers, ctx->d_ees, ctx->d_eas, ctx->d_TL, ctx->d_EU, ctx->d_b,
                     ctx->d_vals, ctx->d_es32, ctx->d_as32, ctx->d_vals32, ctx->d_colind,
-                    ctx->d_self, ctx->d_work};
+                    ctx->d_self, ctx->d_work, ctx->d_rowptr10, ctx->d_boff10, ctx->d_ses,
+                    ctx->d_tlb, ctx->d_kw, ctx->d_Aptr, ctx->d_Astage, ctx->d_Bstage};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int i = 0; i < 8; i++)

@@ -45,4 +45,13 @@ struct vefem_ctx {
     vefem::BatchInst *d_self = nullptr;
     vefem::WorkItem *d_work = nullptr;
     int sms = 0;
+    // linear-stability assembly (10 unknowns per node): pattern and scratch
+    std::vector<int64_t> h_rowptr10;
+    std::vector<int32_t> h_colind10;
+    int64_t *d_rowptr10 = nullptr;
+    int32_t *d_boff10 = nullptr;
+    double *d_ses = nullptr, *d_tlb = nullptr, *d_kw = nullptr;
+    double **d_Aptr = nullptr;
+    double *d_Astage = nullptr, *d_Bstage = nullptr;
+    int stab_nk = 0, stab_nk_stage = 0;
 };

@@ -27,6 +27,7 @@ JACOBIANS = {"fd64": VEFEM_JAC_FD64, "exact64": VEFEM_JAC_EXACT64, "exact32": VE
 VEFEM_ZERO_FIRST = 0x100
 VEFEM_OUTLET_EDGES = 0x200
 VEFEM_TIMING = 0x1000
+VEFEM_STAB_AS_WRITTEN = 0x2000
 
 EXPORTED = ["vefem_abi_version", "vefem_create", "vefem_set_params", "vefem_assemble",
             "vefem_last_timing", "vefem_last_launch_count", "vefem_stream", "vefem_destroy",
@@ -37,7 +38,8 @@ EXPORTED = ["vefem_abi_version", "vefem_create", "vefem_set_params", "vefem_asse
             "vefem_mlp_reset_optimizer", "vefem_mlp_destroy", "vefem_mlp_last_error",
             "vefem_batch_create", "vefem_batch_set_params", "vefem_assemble_batched",
             "vefem_batch_autotune", "vefem_batch_set_tiles", "vefem_batch_info",
-            "vefem_batch_last_timing", "vefem_batch_destroy", "vefem_batch_last_error"]
+            "vefem_batch_last_timing", "vefem_batch_destroy", "vefem_batch_last_error",
+            "vefem_stability_pattern", "vefem_stability_assemble"]
 BATCH_CLASSES = 6
 
 
@@ -110,6 +112,8 @@ def load(path: str = LIB_PATH):
     L.vefem_batch_destroy.argtypes = [P]
     L.vefem_batch_last_error.argtypes = [P]
     L.vefem_batch_last_error.restype = ctypes.c_char_p
+    L.vefem_stability_pattern.argtypes = [P, P, P, P, P]
+    L.vefem_stability_assemble.argtypes = [P, P, I, P, I, P, P, I]
     _lib = L
     return L
 
@@ -249,6 +253,41 @@ class BulkAssembler:
 
     def stream(self) -> int:
         return int(self._L.vefem_stream(self._h) or 0)
+
+    def stability_pattern(self):
+        """AIJ pattern of the stability matrices (10 unknowns per node)."""
+        n, nnz = ctypes.c_int64(), ctypes.c_int64()
+        self._check(self._L.vefem_stability_pattern(self._h, ctypes.byref(n), ctypes.byref(nnz),
+                                                    None, None))
+        rowptr = np.zeros(n.value + 1, dtype=np.int64)
+        colind = np.zeros(nnz.value, dtype=np.int32)
+        self._check(self._L.vefem_stability_pattern(self._h, ctypes.byref(n), ctypes.byref(nnz),
+                                                    rowptr.ctypes.data, colind.ctypes.data))
+        return rowptr, colind
+
+    def stability_assemble(self, TLb, kws, flags: int = VEFEM_ZERO_FIRST, As=None, B=None,
+                           on_device: bool = False):
+        """setEquationsBulkStability for every wavenumber of ``kws``: adds A(k)
+        into As[k] and the k-independent B into B (float64 arrays on the
+        stability pattern; allocated on the host when not given)."""
+        if As is None:
+            _, ci = self.stability_pattern()
+            As = [np.zeros(len(ci)) for _ in kws]
+            if B is None:
+                B = np.zeros(len(ci))
+        kw = np.ascontiguousarray(kws, dtype=np.float64)
+        if on_device:
+            import torch
+            kw_arg = torch.from_numpy(kw).to(f"cuda:{self.device}")
+        else:
+            kw_arg = kw
+        arr = (ctypes.c_void_p * max(1, len(As)))()
+        for i, a in enumerate(As):
+            arr[i] = _ptr(a)
+        tlb = TLb if on_device else np.ascontiguousarray(TLb, dtype=np.float64)
+        self._check(self._L.vefem_stability_assemble(self._h, _ptr(tlb), len(kws), _ptr(kw_arg),
+                                                     flags, arr, _ptr(B), 1 if on_device else 0))
+        return As, B
 
     def close(self):
         if getattr(self, "_h", None):
