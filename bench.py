@@ -26,7 +26,9 @@ unknown (Nex = 1).  Synthetic seeded state (no dataset exists for this path).
   ``--continuation-only --cont-nel N`` runs only this comparison;
 * batched: the batched form, 64 instances of 2,000-20,000 quads at Wi in
   [0.1, 1.0], one persistent launch per kernel replayed as a CUDA graph,
-  against one call per instance.
+  against one call per instance;
+* stability: the linear-stability A/B assembly for 16 spanwise wavenumbers
+  on 20,000 quads (``--stab-nel``), with the CPU oracle on a sample.
 
 ``--impl reference`` times that CPU implementation as the reference arm.
 Multi-GPU: the assembly of one mesh does not shard across GPUs in this
@@ -76,6 +78,8 @@ def parse_args():
                     help="run only the continuation comparison and print its JSON line")
     ap.add_argument("--batch-inst", type=int, default=64,
                     help="instances of the batched-form measurement (0 = skip it)")
+    ap.add_argument("--stab-nel", type=int, default=20000,
+                    help="mesh of the linear-stability measurement (0 = skip it)")
     ap.add_argument("--only", choices=["fd64", "residual", "exact64", "exact32"], default=None,
                     help="time one assembly form alone on the --nel workload (profiling case)")
     return ap.parse_args()
@@ -429,6 +433,56 @@ def run_only(args, asm, mesh, TL, EU, cfg, dev):
     return 0
 
 
+def stability_compare(nel: int, steps: int, warmup: int, device: int = 0, cpu: bool = True):
+    """Linear stability (Oldroyd-B, beta = 0.59, Wi = 0.7, T form): A(k) for
+    16 spanwise wavenumbers uniform in [0, 4] and B, 10 unknowns per node, on
+    a seeded base state; one element launch and one scatter for all k."""
+    import torch
+    mesh = M.build_cylinder_mesh(nel)
+    phys = S.oldroyd_b(0.7, 0.59, "T", nex=0)
+    TL, _ = S.seeded_state(mesh.xyz, phys, seed=0)
+    TLb = np.zeros((10, mesh.nnodes))
+    TLb[0:2] = TL[0:2]
+    TLb[3:7] = TL[2:6]
+    rowptr, colind = V.build_pattern(mesh.conn, mesh.nnodes, 0)
+    asm = V.BulkAssembler(mesh, phys, rowptr, colind, device=device)
+    rp10, ci10 = asm.stability_pattern()
+    d = torch.device(f"cuda:{device}")
+    kws = np.linspace(0.0, 4.0, 16)
+    tA = [torch.zeros(len(ci10), dtype=torch.float64, device=d) for _ in kws]
+    tB = torch.zeros(len(ci10), dtype=torch.float64, device=d)
+    tTLb = torch.from_numpy(TLb).to(d)
+    for _ in range(warmup):
+        asm.stability_assemble(tTLb, kws, V.VEFEM_ZERO_FIRST, tA, tB, on_device=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        asm.stability_assemble(tTLb, kws, V.VEFEM_ZERO_FIRST, tA, tB, on_device=True)
+    torch.cuda.synchronize()
+    sec = (time.perf_counter() - t0) / steps
+    out = {
+        "workload": f"{mesh.nel} Q2 quads, Oldroyd-B beta=0.59 Wi=0.7, T form, seeded base state; "
+                    "A(k) for 16 wavenumbers k in [0, 4] and B, 10 unknowns per node "
+                    f"({len(rp10) - 1} rows, nnz {len(ci10)} per matrix)",
+        "ms_per_assembly": 1e3 * sec, "element_wavenumbers_per_s": mesh.nel * len(kws) / sec,
+        "unit": "element-wavenumber/s", "hbm_bytes_written": 17 * len(ci10) * 8,
+    }
+    asm.close()
+    del tA, tB
+    if cpu:
+        from oracle import oracle as O
+        n = min(mesh.nel, 200)
+        t0 = time.perf_counter()
+        O.stability_elements(phys, mesh.conn, mesh.xyz, TLb, np.zeros_like(TLb), 1.0, e0=0, e1=n,
+                             nthreads=os.cpu_count() or 1)
+        c = time.perf_counter() - t0
+        out["cpu_oracle"] = {"value": n / c, "unit": "element-wavenumber/s",
+                             "cores": os.cpu_count(), "kind": "port",
+                             "sample": f"forward-difference A and B of the first {n} elements "
+                                       "at one wavenumber (element blocks, no scatter)"}
+    return out
+
+
 def run_vefem(args):
     import torch
     world, rank, local, dist = dist_setup()
@@ -584,6 +638,9 @@ def run_vefem(args):
         line["batched"] = batched_compare(args.batch_inst, max(3, args.steps // 2), args.warmup, dev)
     if world == 1 and args.cont_nel > 0:
         line["continuation"] = continuation_compare(args.cont_nel, args.cont_wi, dev)
+    if world == 1 and args.stab_nel > 0:
+        line["stability"] = stability_compare(args.stab_nel, max(3, args.steps // 4), args.warmup,
+                                              dev, cpu=not args.no_cpu_baseline)
     # the CPU baseline runs last: its OpenMP worker threads stay on the host
     # cores afterwards and would slow the host side of the parts above
     if world == 1 and not args.no_cpu_baseline:

@@ -398,14 +398,29 @@ __device__ __forceinline__ int st_q(int f, int s)
     return f < 3 ? f * 4 + s : (f == 3 ? 12 + s : 15 + (f - 4) * 3 + s);
 }
 
+constexpr int ST_JCH = 3;                                            // test nodes per chunk
+constexpr int ST_CH_OUT = ST_JCH * 900;                              // outputs per chunk (2700)
+constexpr int ST_PER_T = (ST_CH_OUT + ST_THREADS - 1) / ST_THREADS;  // outputs per thread (11)
+constexpr int ST_A2 = ST_NQ + 1;                                     // row stride of A2
+
+// Shared memory: D [9][33][10][3] coefficient derivatives of one matrix, A2
+// [30][ST_A2] the test-side contraction of one Gauss point for one chunk of
+// three test nodes, and the base quantities of the 9 Gauss points.
+__host__ __device__ constexpr size_t st_smem_doubles()
+{
+    return (size_t)9 * ST_NQ * ST_NEQ * 3 + (size_t)ST_JCH * ST_NEQ * ST_A2;
+}
+
 __global__ void __launch_bounds__(ST_THREADS)
 k_stability(const StabArgs a, const KParams prm)
 {
     extern __shared__ __align__(16) double sm[];
-    double *D = sm;                                   // [9][33][10][3] for one matrix
-    StabBase *base = reinterpret_cast<StabBase *>(D + 9 * ST_NQ * ST_NEQ * 3);
+    double *D = sm;                                   // [9][33][10][3]
+    double *A2 = D + 9 * ST_NQ * ST_NEQ * 3;          // [30][ST_A2]
+    StabBase *base = reinterpret_cast<StabBase *>(A2 + ST_JCH * ST_NEQ * ST_A2);
     __shared__ double s_tlb[9 * ST_NEQ];
-    __shared__ double s_dFx[9][9], s_dFy[9][9], s_d2x[9][9], s_d2y[9][9], s_H2[9], s_W[9];
+    __shared__ double s_dFx[9][9], s_dFy[9][9], s_lap[9][9], s_H2[9], s_W[9];
+    __shared__ double s_d2x[9][9], s_d2y[9][9];
     const int t = threadIdx.x;
     for (int e = blockIdx.x; e < a.nel; e += gridDim.x) {
         if (t < 9 * ST_NEQ) {
@@ -426,6 +441,7 @@ k_stability(const StabArgs a, const KParams prm)
                 s_dFy[ig][n] = fy[n];
                 s_d2x[ig][n] = sx[n];
                 s_d2y[ig][n] = sy[n];
+                s_lap[ig][n] = sx[n] + sy[n];
             }
             s_H2[ig] = go.H2;
             s_W[ig] = go.WET;
@@ -435,7 +451,9 @@ k_stability(const StabArgs a, const KParams prm)
             stab_base(prm, s_tlb, s_dFx[t], s_dFy[t], s_d2x[t], s_d2y[t], s_H2[t], s_W[t], t, base[t]);
         __syncthreads();
         double *out = a.es + (size_t)e * 4 * ST_BLK;
-        // m = 0: B (from K = 0); m = 1, 2, 3: A at K = 0, +1, -1
+        // element block m: 0 B (K = 0), 1 A(0), 2 A(+1), 3 A(-1); layout
+        // ((jnod*9 + inod)*10 + jeq)*10 + ieq: row (jnod, jeq) = equation of test node
+        // jnod, column (inod, ieq) = unknown of trial node inod
         for (int m = 0; m < 4; m++) {
             const double K = m == 2 ? 1.0 : (m == 3 ? -1.0 : 0.0);
             for (int w = t; w < 9 * ST_NQ; w += ST_THREADS) {
@@ -447,28 +465,45 @@ k_stability(const StabArgs a, const KParams prm)
                     for (int c = 0; c < 3; c++) dst[e2 * 3 + c] = m == 0 ? cb[e2][c] : ca[e2][c];
             }
             __syncthreads();
-            // block layout: ((jnod*9 + inod)*10 + jeq)*10 + ieq; row (jnod, jeq) = equation of
-            // test node jnod, column (inod, ieq) = unknown of trial node inod
-            for (int o = t; o < ST_BLK; o += ST_THREADS) {
-                const int ji = o / 100, r = o % 100;
-                const int jn = ji / 9, in = ji % 9;
-                const int je = r / 10, ie = r % 10;
-                const int ns = ie < 3 ? 4 : 3;
-                double acc = 0.0;
+            for (int j0 = 0; j0 < 9; j0 += ST_JCH) {
+                double acc[ST_PER_T];
+#pragma unroll
+                for (int r = 0; r < ST_PER_T; r++) acc[r] = 0.0;
                 for (int gp = 0; gp < 9; gp++) {
-                    const double ps0 = s_bfn[gp][jn], ps1 = s_dFx[gp][jn], ps2 = s_dFy[gp][jn];
-                    const double chi[4] = {s_bfn[gp][in], s_dFx[gp][in], s_dFy[gp][in],
-                                           s_d2x[gp][in] + s_d2y[gp][in]};
-                    double sg = 0.0;
-                    for (int s = 0; s < ns; s++) {
-                        const double *dd = D + ((size_t)(gp * ST_NQ + st_q(ie, s)) * ST_NEQ + je) * 3;
-                        sg = sg + (ps0 * dd[0] + ps1 * dd[1] + ps2 * dd[2]) * chi[s];
+                    // test side: A2[(jn - j0)*10 + je][q] = WET sum_k psi_k(jn) D[gp][q][je][k]
+                    const double w = base[gp].WET;
+                    for (int it = t; it < ST_JCH * ST_NEQ * ST_NQ; it += ST_THREADS) {
+                        const int row = it / ST_NQ, q = it % ST_NQ;
+                        const int jn = j0 + row / ST_NEQ, je = row % ST_NEQ;
+                        const double *dd = D + ((size_t)(gp * ST_NQ + q) * ST_NEQ + je) * 3;
+                        A2[row * ST_A2 + q] = w * (s_bfn[gp][jn] * dd[0] + s_dFx[gp][jn] * dd[1]
+                                                   + s_dFy[gp][jn] * dd[2]);
                     }
-                    acc = acc + base[gp].WET * sg;
+                    __syncthreads();
+                    // trial side; chunk output c = ((jn - j0)*9 + inod)*100 + jeq*10 + ieq
+#pragma unroll
+                    for (int r = 0; r < ST_PER_T; r++) {
+                        const int c = t + r * ST_THREADS;
+                        if (c < ST_CH_OUT) {
+                            const int ji = c / 100, rr = c % 100;
+                            const int jl = ji / 9, in = ji % 9;
+                            const int je = rr / 10, ie = rr % 10;
+                            const double *a2 = A2 + (jl * ST_NEQ + je) * ST_A2;
+                            const int q0 = st_q(ie, 0);
+                            double v = a2[q0] * s_bfn[gp][in] + a2[q0 + 1] * s_dFx[gp][in]
+                                       + a2[q0 + 2] * s_dFy[gp][in];
+                            if (ie < 3) v = v + a2[q0 + 3] * s_lap[gp][in];
+                            acc[r] = acc[r] + v;
+                        }
+                    }
+                    __syncthreads();
                 }
-                out[(size_t)m * ST_BLK + o] = acc;
+#pragma unroll
+                for (int r = 0; r < ST_PER_T; r++) {
+                    const int c = t + r * ST_THREADS;
+                    if (c < ST_CH_OUT) out[(size_t)m * ST_BLK + j0 * 900 + c] = acc[r];
+                }
             }
-            __syncthreads();
         }
     }
 }
@@ -668,7 +703,7 @@ extern "C" int vefem_stability_assemble(vefem_ctx *ctx, const double *TLb, int n
     a.TLb = ctx->d_tlb;
     a.es = ctx->d_ses;
     a.kz = (flags & VEFEM_STAB_AS_WRITTEN) ? 0 : 1;
-    const size_t smem = sizeof(double) * 9 * ST_NQ * ST_NEQ * 3 + 9 * sizeof(StabBase);
+    const size_t smem = sizeof(double) * st_smem_doubles() + 9 * sizeof(StabBase);
     SCK(cudaFuncSetAttribute(k_stability, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int occ = 0;
     SCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_stability, ST_THREADS, smem));
