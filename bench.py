@@ -80,7 +80,8 @@ def parse_args():
                     help="instances of the batched-form measurement (0 = skip it)")
     ap.add_argument("--stab-nel", type=int, default=20000,
                     help="mesh of the linear-stability measurement (0 = skip it)")
-    ap.add_argument("--only", choices=["fd64", "residual", "exact64", "exact32"], default=None,
+    ap.add_argument("--only", choices=["fd64", "residual", "exact64", "exact32", "stability"],
+                    default=None,
                     help="time one assembly form alone on the --nel workload (profiling case)")
     return ap.parse_args()
 
@@ -489,6 +490,12 @@ def run_vefem(args):
     dev = local
     torch.cuda.set_device(dev)
     B.build()
+    if args.only == "stability":
+        if rank == 0:
+            print(json.dumps({"only": "stability",
+                              "stability": stability_compare(args.nel, args.steps, args.warmup, dev,
+                                                             cpu=False)}))
+        return 0
     if args.continuation_only:
         if rank == 0:
             out = continuation_compare(args.cont_nel, args.cont_wi, dev)

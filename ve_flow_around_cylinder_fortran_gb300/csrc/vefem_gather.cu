@@ -138,13 +138,29 @@ __device__ __forceinline__ int find_inst(const int64_t *__restrict__ off, int ni
     return lo;
 }
 
+// Instance of index u: one binary search per CTA (for its first index), then
+// a forward walk, which is empty unless the CTA straddles an instance boundary.
+__device__ __forceinline__ int block_inst(const int64_t *__restrict__ off, int ninst, int64_t u,
+                                         int64_t total)
+{
+    __shared__ int s_first;
+    if (threadIdx.x == 0) {
+        const int64_t u0 = (int64_t)blockIdx.x * blockDim.x;
+        s_first = find_inst(off, ninst, u0 < total ? u0 : total - 1);
+    }
+    __syncthreads();
+    int i = s_first;
+    while (i + 1 < ninst && off[i + 1] <= u) i++;
+    return i;
+}
+
 __global__ void k_gather_residual_batched(const BatchInst *__restrict__ insts,
                                           const int64_t *__restrict__ off, int ninst,
                                           int64_t total)
 {
     const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = block_inst(off, ninst, u, total);
     if (u >= total) return;
-    const int i = find_inst(off, ninst, u);
     const int64_t t = u - off[i];
     const int32_t *nptr = insts[i].ga.nptr, *ncon = insts[i].ga.ncon;
     const double *rs = insts[i].ea.rs;
@@ -162,8 +178,8 @@ __global__ void k_gather_jacobian_batched(const BatchInst *__restrict__ insts,
                                           int64_t total)
 {
     const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = block_inst(off, ninst, u, total);
     if (u >= total) return;
-    const int i = find_inst(off, ninst, u);
     const int64_t t = u - off[i];
     const GatherArgs g = insts[i].ga;
     const T *es = static_cast<const T *>(insts[i].es);
@@ -184,8 +200,8 @@ __global__ void k_gather_arclength_batched(const BatchInst *__restrict__ insts,
                                            int64_t total)
 {
     const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = block_inst(off, ninst, u, total);
     if (u >= total) return;
-    const int i = find_inst(off, ninst, u);
     const int64_t t = u - off[i];
     const GatherArgs g = insts[i].ga;
     if (g.nex == 0) return;
