@@ -74,6 +74,8 @@ def parse_args():
     ap.add_argument("--cont-nel", type=int, default=500,
                     help="mesh of the continuation comparison (0 = skip it)")
     ap.add_argument("--cont-wi", type=float, default=1.0, help="Wi the continuation ends at")
+    ap.add_argument("--no-secant", action="store_true",
+                    help="leave out the secant-predictor arm of the continuation comparison")
     ap.add_argument("--continuation-only", action="store_true",
                     help="run only the continuation comparison and print its JSON line")
     ap.add_argument("--batch-inst", type=int, default=64,
@@ -498,7 +500,8 @@ def run_vefem(args):
         return 0
     if args.continuation_only:
         if rank == 0:
-            out = continuation_compare(args.cont_nel, args.cont_wi, dev)
+            out = continuation_compare(args.cont_nel, args.cont_wi, dev,
+                                       secant=not args.no_secant)
             print(json.dumps({"continuation": out}))
         if dist:
             dist.destroy_process_group()
@@ -644,7 +647,8 @@ def run_vefem(args):
     if world == 1 and args.batch_inst > 0:
         line["batched"] = batched_compare(args.batch_inst, max(3, args.steps // 2), args.warmup, dev)
     if world == 1 and args.cont_nel > 0:
-        line["continuation"] = continuation_compare(args.cont_nel, args.cont_wi, dev)
+        line["continuation"] = continuation_compare(args.cont_nel, args.cont_wi, dev,
+                                                    secant=not args.no_secant)
     if world == 1 and args.stab_nel > 0:
         line["stability"] = stability_compare(args.stab_nel, max(3, args.steps // 4), args.warmup,
                                               dev, cpu=not args.no_cpu_baseline)

@@ -140,16 +140,23 @@ __device__ __forceinline__ int find_inst(const int64_t *__restrict__ off, int ni
 
 // Instance of index u: one binary search per CTA (for its first index), then
 // a forward walk, which is empty unless the CTA straddles an instance boundary.
-__device__ __forceinline__ int block_inst(const int64_t *__restrict__ off, int ninst, int64_t u,
-                                         int64_t total)
+// The first instance's descriptor is staged in shared memory for the CTA.
+struct BlockInst {
+    int first;
+    BatchInst d;
+};
+
+__device__ __forceinline__ int block_inst(const BatchInst *__restrict__ insts,
+                                         const int64_t *__restrict__ off, int ninst, int64_t u,
+                                         int64_t total, BlockInst &sb)
 {
-    __shared__ int s_first;
     if (threadIdx.x == 0) {
         const int64_t u0 = (int64_t)blockIdx.x * blockDim.x;
-        s_first = find_inst(off, ninst, u0 < total ? u0 : total - 1);
+        sb.first = find_inst(off, ninst, u0 < total ? u0 : total - 1);
+        sb.d = insts[sb.first];
     }
     __syncthreads();
-    int i = s_first;
+    int i = sb.first;
     while (i + 1 < ninst && off[i + 1] <= u) i++;
     return i;
 }
@@ -158,13 +165,15 @@ __global__ void k_gather_residual_batched(const BatchInst *__restrict__ insts,
                                           const int64_t *__restrict__ off, int ninst,
                                           int64_t total)
 {
+    __shared__ BlockInst sb;
     const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = block_inst(off, ninst, u, total);
+    const int i = block_inst(insts, off, ninst, u, total, sb);
     if (u >= total) return;
+    const BatchInst &I = (i == sb.first) ? sb.d : insts[i];
     const int64_t t = u - off[i];
-    const int32_t *nptr = insts[i].ga.nptr, *ncon = insts[i].ga.ncon;
-    const double *rs = insts[i].ea.rs;
-    double *b = insts[i].b;
+    const int32_t *nptr = I.ga.nptr, *ncon = I.ga.ncon;
+    const double *rs = I.ea.rs;
+    double *b = I.b;
     const int node = (int)(t / 6), jeq = (int)(t - (int64_t)node * 6);
     double acc = b[t];
     const int c0 = nptr[node], c1 = nptr[node + 1];
@@ -177,13 +186,15 @@ __global__ void k_gather_jacobian_batched(const BatchInst *__restrict__ insts,
                                           const int64_t *__restrict__ off, int ninst,
                                           int64_t total)
 {
+    __shared__ BlockInst sb;
     const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = block_inst(off, ninst, u, total);
+    const int i = block_inst(insts, off, ninst, u, total, sb);
     if (u >= total) return;
+    const BatchInst &I = (i == sb.first) ? sb.d : insts[i];
     const int64_t t = u - off[i];
-    const GatherArgs g = insts[i].ga;
-    const T *es = static_cast<const T *>(insts[i].es);
-    T *vals = static_cast<T *>(insts[i].vals);
+    const GatherArgs &g = I.ga;
+    const T *es = static_cast<const T *>(I.es);
+    T *vals = static_cast<T *>(I.vals);
     const int blk = (int)(t / 36);
     const int r = (int)(t - (int64_t)blk * 36);
     const int jeq = r / 6, ieq = r - 6 * (r / 6);
@@ -199,14 +210,16 @@ __global__ void k_gather_arclength_batched(const BatchInst *__restrict__ insts,
                                            const int64_t *__restrict__ off, int ninst,
                                            int64_t total)
 {
+    __shared__ BlockInst sb;
     const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = block_inst(off, ninst, u, total);
+    const int i = block_inst(insts, off, ninst, u, total, sb);
     if (u >= total) return;
+    const BatchInst &I = (i == sb.first) ? sb.d : insts[i];
     const int64_t t = u - off[i];
-    const GatherArgs g = insts[i].ga;
+    const GatherArgs &g = I.ga;
     if (g.nex == 0) return;
-    const T *as = static_cast<const T *>(insts[i].as);
-    T *vals = static_cast<T *>(insts[i].vals);
+    const T *as = static_cast<const T *>(I.as);
+    T *vals = static_cast<T *>(I.vals);
     const int node = (int)(t / 6), jeq = (int)(t - (int64_t)node * 6);
     const int64_t slot = g.rowptr[t + 1] - 1;
     T acc = vals[slot];

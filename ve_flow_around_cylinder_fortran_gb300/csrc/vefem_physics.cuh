@@ -12,6 +12,8 @@
 
 #include <math.h>
 
+#include <type_traits>
+
 #include "vefem_internal.h"
 #include "vefem_scalar.cuh"
 
@@ -22,6 +24,40 @@
 #endif
 
 namespace vefem {
+
+// Divisions that share a divisor (the SQRT-form test-function terms divide by
+// S11 + S22 and by Wi at every test node).  For FP64 on the device they use
+// Markstein's method (P. Markstein, "Computation of elementary functions on
+// the IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1), 1990): with
+// r the correctly rounded reciprocal of y and q0 = RN(x r) within one ulp of
+// x / y, the remainder e = x - q0 y is exact by FMA and RN(q0 + e r) is the
+// correctly rounded quotient, i.e. the IEEE division's result, for operands
+// and quotients in the normal range (the case here).  Other value types
+// divide plainly.
+template <class R>
+VF_HD R recip_for_div(R y)
+{
+#ifdef __CUDA_ARCH__
+    if constexpr (std::is_same<R, double>::value) return __drcp_rn(y);
+#endif
+    return y;   // unused by div_r below
+}
+
+template <class R>
+VF_HD R div_r(R x, R y, R r)
+{
+#ifdef __CUDA_ARCH__
+    if constexpr (std::is_same<R, double>::value) {
+        const double q0 = x * r;
+        if (q0 == 0.0) return q0;                   // keeps the sign of a zero quotient
+        const double e = __fma_rn(-q0, y, x);
+        return __fma_rn(e, r, q0);
+    }
+#endif
+    (void)r;
+    return x / y;
+}
+
 
 // FORM_T / FORM_SQRT and the specialisations SPEC_RE0 / SPEC_DF0 are in
 // vefem_internal.h.
@@ -96,6 +132,7 @@ struct GpCoef {
     R tlsme, tlsic, ntl, tlsce, tdcs, mag;
     R C11, C12, C21, C22;   // Con_EQ
     R S11, S12, S22, den;   // SQRT form: S and S11 + S22
+    R rden, rWi;            // reciprocals for div_r (FP64 on the device; unused otherwise)
     R WiN, fT, omb;
     R dS11x, dS11y, dS12x, dS12y, dS22x, dS22y;
 };
@@ -383,6 +420,8 @@ VF_HD GpCoef<R> gauss_point(const Interp<R> &I, const KParams &prm, R WiN, G H2,
         ddS = ((S11 * S11 + S12 * S12) + S12 * S12) + S22 * S22;
         ddC = ((Cc11 * Cc11 + Cc12 * Cc12) + Cc12 * Cc12) + Cc22 * Cc22;
         g.den = den;
+        g.rden = recip_for_div(den);
+        g.rWi = recip_for_div(WiN);
     }
     g.fT = fT;
     g.C11 = C11; g.C12 = C12; g.C21 = C21; g.C22 = C22;
@@ -475,23 +514,24 @@ VF_HD void test_node(const GpCoef<R> &g, const KParams &prm, B bifn, G fx, G fy,
         const R S11 = g.S11, S12 = g.S12, S22 = g.S22;
         const R m1a = S11 * fx + S12 * fy;   // (S . grad phi)_1
         const R m1b = S12 * fx + S22 * fy;   // (S . grad phi)_2
-        const R wa = m1b / g.den;            // W12 for i = 1
-        const R wb = -(m1a / g.den);         // W12 for i = 2
+        const R wa = div_r(m1b, g.den, g.rden);          // W12 for i = 1
+        const R wb = -div_r(m1a, g.den, g.rden);         // W12 for i = 2
         const R k = g.tlsce;
         const R omb = g.omb, Wi = g.WiN;
         // i = 1: GU_lsce column 1 = grad phi
         R u11 = -m1a - wa * S12, u12 = -(wa * S22);
         R u21 = -m1b - (-wa) * S11, u22 = -((-wa) * S12);
-        R l11 = k * u11 * omb / Wi, l12 = k * u12 * omb / Wi;
-        R l21 = k * u21 * omb / Wi, l22 = k * u22 * omb / Wi;
+        const R rW = g.rWi;
+        R l11 = div_r(k * u11 * omb, Wi, rW), l12 = div_r(k * u12 * omb, Wi, rW);
+        R l21 = div_r(k * u21 * omb, Wi, rW), l22 = div_r(k * u22 * omb, Wi, rW);
         lsce1 = ((l11 * g.C11 + l12 * g.C21) + l21 * g.C12) + l22 * g.C22;
         // i = 2: GU_lsce column 2 = grad phi
         u11 = -(wb * S12);
         u12 = -m1a - wb * S22;
         u21 = -((-wb) * S11);
         u22 = -m1b - (-wb) * S12;
-        l11 = k * u11 * omb / Wi; l12 = k * u12 * omb / Wi;
-        l21 = k * u21 * omb / Wi; l22 = k * u22 * omb / Wi;
+        l11 = div_r(k * u11 * omb, Wi, rW); l12 = div_r(k * u12 * omb, Wi, rW);
+        l21 = div_r(k * u21 * omb, Wi, rW); l22 = div_r(k * u22 * omb, Wi, rW);
         lsce2 = ((l11 * g.C11 + l12 * g.C21) + l21 * g.C12) + l22 * g.C22;
     }
     const R pd1 = g.P11 * fx + g.P12 * fy;

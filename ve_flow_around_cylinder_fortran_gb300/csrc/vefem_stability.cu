@@ -531,9 +531,9 @@ __global__ void k_stability_gather(const GatherArgs g, const int64_t *__restrict
     }
     if (B) B[slot] = B[slot] + sb;
     const double a1 = (sp - sn) * 0.5, a2 = (sp + sn) * 0.5 - s0;
-    for (int k = 0; k < nk; k++) {
+    for (int k = 0; k < nk; k++) {   // A(K) = s0 + K (a1 + K a2), two FMAs per wavenumber
         const double K = kw[k];
-        A[k][slot] = A[k][slot] + (s0 + K * a1 + (K * K) * a2);
+        A[k][slot] = A[k][slot] + __fma_rn(K, __fma_rn(K, a2, a1), s0);
     }
 }
 
