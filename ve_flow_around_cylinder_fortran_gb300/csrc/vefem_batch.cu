@@ -2,12 +2,14 @@
 // per kernel, captured once in a CUDA graph and replayed.
 //
 // Each instance keeps the tables of a single-mesh context (vefem_create); the
-// batch adds one descriptor per instance in device memory (BatchInst), a work
-// list of (instance, first element, count) items for the element kernels, and
-// prefix offsets of the instances' residual rows and block entries for the
-// scatter kernels.  The element kernels run with a grid of SMs x resident
-// CTAs and walk the work list with a grid stride; the element-batch tile
-// (elements per work item) is chosen per mesh-size class by the autotuner.
+// batch adds one descriptor per instance in device memory (BatchInst) and a
+// work list of (instance, first element, count) items for the element
+// kernels, which run with a grid of SMs x resident CTAs and walk the work list
+// with a grid stride; the element-batch tile (elements per work item) is
+// chosen per mesh-size class by the autotuner.  The scatter is the single-mesh
+// element-ordered gather per instance, captured as graph nodes (a single
+// scatter over all instances measured slower: each thread had to find its
+// instance and load its tables).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -57,8 +59,6 @@ struct vefem_batch {
     // descriptors and index spaces
     std::vector<BatchInst> h_inst;
     BatchInst *d_inst = nullptr;
-    std::vector<int64_t> h_row_off, h_blk_off;
-    int64_t *d_row_off = nullptr, *d_blk_off = nullptr;
     WorkItem *d_res_work = nullptr, *d_ex_work = nullptr;
     int n_res_work = 0, n_ex_work = 0;
     int64_t total_el = 0;
@@ -169,19 +169,27 @@ void launch_all(vefem_batch *bt, int flags, bool timing, cudaError_t *err)
         bt->launches++;
     }
     if (timing && e == cudaSuccess) e = cudaEventRecord(bt->ev[2], s);
-    const int64_t rows = bt->h_row_off[bt->ninst], blks = bt->h_blk_off[bt->ninst];
-    if (want_res && e == cudaSuccess) {
-        e = launch_gather_residual_batched(bt->d_inst, bt->d_row_off, bt->ninst, rows, s);
-        bt->launches++;
-    }
-    if (jmode && e == cudaSuccess) {
-        e = f32 ? launch_gather_jacobian_batched<float>(bt->d_inst, bt->d_blk_off, bt->ninst, blks, s)
-                : launch_gather_jacobian_batched<double>(bt->d_inst, bt->d_blk_off, bt->ninst, blks, s);
-        bt->launches++;
-        if (bt->nex && e == cudaSuccess) {
-            e = f32 ? launch_gather_arclength_batched<float>(bt->d_inst, bt->d_row_off, bt->ninst, rows, s)
-                    : launch_gather_arclength_batched<double>(bt->d_inst, bt->d_row_off, bt->ninst, rows, s);
+    // scatter: the single-mesh element-ordered gathers, one launch per instance and
+    // array (graph nodes), with each instance's tables as kernel arguments
+    for (int i = 0; i < bt->ninst && e == cudaSuccess; i++) {
+        const BatchInst &I = bt->h_inst[i];
+        if (want_res) {
+            e = launch_gather_residual(I.ga, I.ea.rs, I.b, s);
             bt->launches++;
+        }
+        if (jmode && e == cudaSuccess) {
+            e = f32 ? launch_gather_jacobian32(I.ga, static_cast<const float *>(I.es),
+                                               static_cast<float *>(I.vals), s)
+                    : launch_gather_jacobian(I.ga, static_cast<const double *>(I.es),
+                                             static_cast<double *>(I.vals), s);
+            bt->launches++;
+            if (bt->nex && e == cudaSuccess) {
+                e = f32 ? launch_gather_arclength32(I.ga, static_cast<const float *>(I.as),
+                                                    static_cast<float *>(I.vals), s)
+                        : launch_gather_arclength(I.ga, static_cast<const double *>(I.as),
+                                                  static_cast<double *>(I.vals), s);
+                bt->launches++;
+            }
         }
     }
     if (timing && e == cudaSuccess) e = cudaEventRecord(bt->ev[3], s);
@@ -227,17 +235,7 @@ extern "C" int vefem_batch_create(int ninst, const vefem_mesh *meshes, const vef
         BCK(cudaDeviceGetAttribute(&bt->sms, cudaDevAttrMultiProcessorCount, bt->device));
         BCK(cudaStreamCreateWithFlags(&bt->s, cudaStreamNonBlocking));
         for (auto &ev : bt->ev) BCK(cudaEventCreate(&ev));
-        bt->h_row_off.assign(ninst + 1, 0);
-        bt->h_blk_off.assign(ninst + 1, 0);
-        for (int i = 0; i < ninst; i++) {
-            bt->h_row_off[i + 1] = bt->h_row_off[i] + (int64_t)bt->ctx[i]->nnodes * 6;
-            bt->h_blk_off[i + 1] = bt->h_blk_off[i] + (int64_t)bt->ctx[i]->nblocks * 36;
-            bt->total_el += bt->ctx[i]->nel;
-        }
-        BCK(cudaMalloc(&bt->d_row_off, (ninst + 1) * sizeof(int64_t)));
-        BCK(cudaMalloc(&bt->d_blk_off, (ninst + 1) * sizeof(int64_t)));
-        BCK(cudaMemcpy(bt->d_row_off, bt->h_row_off.data(), (ninst + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
-        BCK(cudaMemcpy(bt->d_blk_off, bt->h_blk_off.data(), (ninst + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
+        for (int i = 0; i < ninst; i++) bt->total_el += bt->ctx[i]->nel;
         BCK(cudaMalloc(&bt->d_inst, ninst * sizeof(BatchInst)));
         bt->h_inst.resize(ninst);
         for (int i = 0; i < ninst; i++) {
@@ -259,8 +257,6 @@ extern "C" int vefem_batch_create(int ninst, const vefem_mesh *meshes, const vef
             I.ga.boff = c->d_boff;
             I.ga.bptr = c->d_bptr;
             I.ga.bcon = c->d_bcon;
-            I.row0 = bt->h_row_off[i];
-            I.blk0 = bt->h_blk_off[i];
         }
         return build_work(bt);
     };
@@ -560,7 +556,7 @@ extern "C" int vefem_batch_destroy(vefem_batch *bt)
     if (bt->s) cudaStreamSynchronize(bt->s);
     if (bt->graph) cudaGraphExecDestroy(bt->graph);
     for (vefem_ctx *c : bt->ctx) vefem_destroy(c);
-    void *p[] = {bt->d_inst, bt->d_row_off, bt->d_blk_off, bt->d_res_work, bt->d_ex_work,
+    void *p[] = {bt->d_inst, bt->d_res_work, bt->d_ex_work,
                  bt->d_rs, bt->d_es, bt->d_as};
     for (void *q : p)
         if (q) cudaFree(q);

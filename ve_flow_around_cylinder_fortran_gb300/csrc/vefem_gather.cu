@@ -124,146 +124,4 @@ cudaError_t launch_gather_arclength(const GatherArgs &g, const double *as, doubl
     return cudaGetLastError();
 }
 
-// ---------------------------------------------------------------------------
-// Batched form: one launch over the rows (or block entries) of many meshes.
-// off[ninst + 1] are the prefix offsets of the instances in that index space.
-
-__device__ __forceinline__ int find_inst(const int64_t *__restrict__ off, int ninst, int64_t t)
-{
-    int lo = 0, hi = ninst;          // off[lo] <= t < off[hi]
-    while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (off[mid] <= t) lo = mid; else hi = mid;
-    }
-    return lo;
-}
-
-// Instance of index u: one binary search per CTA (for its first index), then
-// a forward walk, which is empty unless the CTA straddles an instance boundary.
-// The first instance's descriptor is staged in shared memory for the CTA.
-struct BlockInst {
-    int first;
-    BatchInst d;
-};
-
-__device__ __forceinline__ int block_inst(const BatchInst *__restrict__ insts,
-                                         const int64_t *__restrict__ off, int ninst, int64_t u,
-                                         int64_t total, BlockInst &sb)
-{
-    if (threadIdx.x == 0) {
-        const int64_t u0 = (int64_t)blockIdx.x * blockDim.x;
-        sb.first = find_inst(off, ninst, u0 < total ? u0 : total - 1);
-        sb.d = insts[sb.first];
-    }
-    __syncthreads();
-    int i = sb.first;
-    while (i + 1 < ninst && off[i + 1] <= u) i++;
-    return i;
-}
-
-__global__ void k_gather_residual_batched(const BatchInst *__restrict__ insts,
-                                          const int64_t *__restrict__ off, int ninst,
-                                          int64_t total)
-{
-    __shared__ BlockInst sb;
-    const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = block_inst(insts, off, ninst, u, total, sb);
-    if (u >= total) return;
-    const BatchInst &I = (i == sb.first) ? sb.d : insts[i];
-    const int64_t t = u - off[i];
-    const int32_t *nptr = I.ga.nptr, *ncon = I.ga.ncon;
-    const double *rs = I.ea.rs;
-    double *b = I.b;
-    const int node = (int)(t / 6), jeq = (int)(t - (int64_t)node * 6);
-    double acc = b[t];
-    const int c0 = nptr[node], c1 = nptr[node + 1];
-    for (int c = c0; c < c1; c++) acc = acc + rs[(int64_t)ncon[c] * 6 + jeq];
-    b[t] = acc;
-}
-
-template <class T>
-__global__ void k_gather_jacobian_batched(const BatchInst *__restrict__ insts,
-                                          const int64_t *__restrict__ off, int ninst,
-                                          int64_t total)
-{
-    __shared__ BlockInst sb;
-    const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = block_inst(insts, off, ninst, u, total, sb);
-    if (u >= total) return;
-    const BatchInst &I = (i == sb.first) ? sb.d : insts[i];
-    const int64_t t = u - off[i];
-    const GatherArgs &g = I.ga;
-    const T *es = static_cast<const T *>(I.es);
-    T *vals = static_cast<T *>(I.vals);
-    const int blk = (int)(t / 36);
-    const int r = (int)(t - (int64_t)blk * 36);
-    const int jeq = r / 6, ieq = r - 6 * (r / 6);
-    const int64_t slot = g.rowptr[(int64_t)g.brow[blk] * 6 + jeq] + g.boff[blk] + ieq;
-    T acc = vals[slot];
-    const int c0 = g.bptr[blk], c1 = g.bptr[blk + 1];
-    for (int c = c0; c < c1; c++) acc = acc + es[(int64_t)g.bcon[c] * 36 + r];
-    vals[slot] = acc;
-}
-
-template <class T>
-__global__ void k_gather_arclength_batched(const BatchInst *__restrict__ insts,
-                                           const int64_t *__restrict__ off, int ninst,
-                                           int64_t total)
-{
-    __shared__ BlockInst sb;
-    const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = block_inst(insts, off, ninst, u, total, sb);
-    if (u >= total) return;
-    const BatchInst &I = (i == sb.first) ? sb.d : insts[i];
-    const int64_t t = u - off[i];
-    const GatherArgs &g = I.ga;
-    if (g.nex == 0) return;
-    const T *as = static_cast<const T *>(I.as);
-    T *vals = static_cast<T *>(I.vals);
-    const int node = (int)(t / 6), jeq = (int)(t - (int64_t)node * 6);
-    const int64_t slot = g.rowptr[t + 1] - 1;
-    T acc = vals[slot];
-    const int c0 = g.nptr[node], c1 = g.nptr[node + 1];
-    for (int c = c0; c < c1; c++) acc = acc + as[(int64_t)g.ncon[c] * 6 + jeq];
-    vals[slot] = acc;
-}
-
-cudaError_t launch_gather_residual_batched(const BatchInst *insts, const int64_t *row_off,
-                                           int ninst, int64_t total, cudaStream_t s)
-{
-    if (total <= 0) return cudaSuccess;
-    k_gather_residual_batched<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(insts, row_off,
-                                                                              ninst, total);
-    return cudaGetLastError();
-}
-
-template <class T>
-cudaError_t launch_gather_jacobian_batched(const BatchInst *insts, const int64_t *blk_off,
-                                           int ninst, int64_t total, cudaStream_t s)
-{
-    if (total <= 0) return cudaSuccess;
-    k_gather_jacobian_batched<T><<<(unsigned)((total + 287) / 288), 288, 0, s>>>(insts, blk_off,
-                                                                                 ninst, total);
-    return cudaGetLastError();
-}
-
-template <class T>
-cudaError_t launch_gather_arclength_batched(const BatchInst *insts, const int64_t *row_off,
-                                            int ninst, int64_t total, cudaStream_t s)
-{
-    if (total <= 0) return cudaSuccess;
-    k_gather_arclength_batched<T><<<(unsigned)((total + 255) / 256), 256, 0, s>>>(insts, row_off,
-                                                                                  ninst, total);
-    return cudaGetLastError();
-}
-
-template cudaError_t launch_gather_jacobian_batched<float>(const BatchInst *, const int64_t *,
-                                                           int, int64_t, cudaStream_t);
-template cudaError_t launch_gather_jacobian_batched<double>(const BatchInst *, const int64_t *,
-                                                            int, int64_t, cudaStream_t);
-template cudaError_t launch_gather_arclength_batched<float>(const BatchInst *, const int64_t *,
-                                                            int, int64_t, cudaStream_t);
-template cudaError_t launch_gather_arclength_batched<double>(const BatchInst *, const int64_t *,
-                                                             int, int64_t, cudaStream_t);
-
 }  // namespace vefem

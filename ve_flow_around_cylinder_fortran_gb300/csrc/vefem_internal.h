@@ -110,8 +110,6 @@ struct BatchInst {
     void *es, *as;        // element Jacobian / arclength scratch (T of the launch)
     double *b;            // residual (device)
     void *vals;           // AIJ values (T of the launch)
-    int64_t row0;         // first residual row of this instance in the row space (nnodes*6)
-    int64_t blk0;         // first block entry of this instance (nblocks*36)
 };
 struct WorkItem {
     int inst, e0, count, pad;
@@ -121,16 +119,6 @@ cudaError_t launch_residual64_batched(const BatchInst *insts, const WorkItem *wo
 template <class T>
 cudaError_t launch_exact_batched(const BatchInst *insts, const WorkItem *work, int nwork,
                                  int form, int spec, int grid, cudaStream_t s);
-// residual rows / block entries / arclength rows of all instances:
-// total = sum over instances; offsets [ninst + 1] are row0 (or blk0) prefixes
-cudaError_t launch_gather_residual_batched(const BatchInst *insts, const int64_t *row_off,
-                                           int ninst, int64_t total, cudaStream_t s);
-template <class T>
-cudaError_t launch_gather_jacobian_batched(const BatchInst *insts, const int64_t *blk_off,
-                                           int ninst, int64_t total, cudaStream_t s);
-template <class T>
-cudaError_t launch_gather_arclength_batched(const BatchInst *insts, const int64_t *row_off,
-                                            int ninst, int64_t total, cudaStream_t s);
 // occupancy of the persistent kernels (resident CTAs per SM)
 int exact_batched_ctas_per_sm(int elem_size, int form, int spec);
 int residual_batched_ctas_per_sm(int form);
