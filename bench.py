@@ -266,9 +266,10 @@ def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=Non
     """Arclength continuation Wi 0.1 -> wi_end (Oldroyd-B, beta = 0.59, SQRT
     form) on the GPU assembly, arms from the same start: the plain FP64 path
     (FD64 Jacobian, the reference's tangent predictor), the same with a
-    secant predictor, and the learned + mixed path (FP32 exact Jacobian with
-    FP64 residual, learned POD/MLP predictor trained online after the first
-    20 points).  Every point is converged to
+    secant predictor, the learned + mixed path (FP32 exact Jacobian with FP64
+    residual, learned POD/MLP predictor trained online after the first 20
+    points), and the same without the network (its reduced-space quadratic
+    extrapolation alone: the ablation).  Every point is converged to
     ||R|| < 1e-10 and ||dx|| < 1e-10; host wall time per arm."""
     from ve_flow_around_cylinder_fortran_gb300 import continuation as C
     from ve_flow_around_cylinder_fortran_gb300 import learned as LP
@@ -280,29 +281,34 @@ def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=Non
     asm = V.BulkAssembler(mesh, phys, rowptr, colind, outlet_edges=True, device=device)
     cfg = C.ArclengthSettings(dArN=0.01, lam_max=wi_end / phys.Wi0, max_steps=2000)
     arms, states = {}, {}
-    runs = [("plain_fp64", "fd64", None), ("learned_fp32", "exact32", "learned")]
+    runs = [("plain_fp64", "fd64", None), ("learned_fp32", "exact32", "learned"),
+            ("pod_quadratic_fp32", "exact32", "ablate")]
     if secant:
         runs.insert(1, ("secant_fp64", "fd64", "secant"))
     for name, jac, kind in runs:
         cont = C.ArclengthContinuation(asm, mesh, phys, jac, cfg)
         pred = None
-        if kind == "learned":
-            pred = LP.LearnedPredictor(n_modes=32, start=20, device=f"cuda:{device}")
+        if kind in ("learned", "ablate"):
+            pred = LP.LearnedPredictor(n_modes=32, start=20, device=f"cuda:{device}",
+                                       use_net=kind == "learned")
         elif kind == "secant":
             pred = C.SecantPredictor()
         t0 = time.perf_counter()
         recs, xs = cont.run(TL, EU, predictor=pred)
         wall = time.perf_counter() - t0
-        if kind == "learned":
+        if kind in ("learned", "ablate"):
             pred.net.close()
         states[name] = xs
         arms[name] = {
             "jacobian": jac,
-            "predictor": {"learned": "learned POD/MLP", "secant": "secant", None: "tangent"}[kind],
+            "predictor": {"learned": "learned POD/MLP", "secant": "secant", None: "tangent",
+                          "ablate": "POD quadratic extrapolation, network off"}[kind],
             "wall_s": wall, "steps": len(recs), "steps_per_s": len(recs) / wall,
             "newton_iterations": sum(r.newton_iterations for r in recs),
             "factorisations": sum(r.factorisations for r in recs),
             "learned_taken": sum(r.predictor == "learned" for r in recs),
+            "mean_err_pr_after_20": float(np.mean([r.pred_error for r in recs[20:]]))
+            if len(recs) > 20 else None,
             "emergency_restarts": sum(r.emergencies for r in recs),
             "final_wi": recs[-1].wi, "max_final_res_norm": max(r.res_norm for r in recs),
             "time_split_s": {"assembly": sum(r.assembly_s for r in recs),
@@ -311,7 +317,7 @@ def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=Non
                              "predictor": sum(r.predictor_s for r in recs)},
             "mean_dS_after_20": float(np.mean([r.dS for r in recs[20:]])) if len(recs) > 20 else None,
         }
-        if kind == "learned":
+        if kind in ("learned", "ablate"):
             arms[name]["predictor_split_s"] = dict(pred.timers, judge=cont.judge_s)
         if log:
             log(f"{name}: {arms[name]}")

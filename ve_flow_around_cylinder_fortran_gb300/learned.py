@@ -43,7 +43,7 @@ import numpy as np
 class LearnedPredictor:
     def __init__(self, n_modes: int = 32, start: int = 20, width: int = 256, hidden: int = 3,
                  iters: int = 400, lr: float = 1.0e-3, seed: int = 0, device: str = "cuda:0",
-                 net=None, log=None):
+                 net=None, log=None, use_net: bool = True):
         import torch
         self.torch = torch
         self.dev = torch.device(device)
@@ -65,6 +65,9 @@ class LearnedPredictor:
         self.last_loss = None
         self.trainings = 0
         self.timers = {"pod": 0.0, "train": 0.0, "predict": 0.0}
+        # use_net = False: the ablation without the network (the reduced-space
+        # quadratic extrapolation alone)
+        self.use_net = use_net
 
     # ---- data --------------------------------------------------------------
     def observe(self, k: int, x: np.ndarray, wi: float):
@@ -138,8 +141,9 @@ class LearnedPredictor:
         xs = np.where(xs > 1e-12 * max(1.0, np.abs(xm).max()), xs, 1.0)
         ys = np.where(ys > 1e-30, ys, 1.0)
         self.norm = (xm, xs, ym, ys)
-        self.net.reset_optimizer()
-        self.last_loss = self.net.train((X - xm) / xs, (Y - ym) / ys, self.iters, self.lr)
+        if self.use_net:
+            self.net.reset_optimizer()
+            self.last_loss = self.net.train((X - xm) / xs, (Y - ym) / ys, self.iters, self.lr)
         self.trainings += 1
         self.timers["pod"] += t1 - t0
         self.timers["train"] += time.perf_counter() - t1
@@ -158,7 +162,10 @@ class LearnedPredictor:
         coef = self.coef
         f, quad = self._features(m, dS, coef)
         xm, xs, ym, ys = self.norm
-        dy = self.net.forward(((f - xm) / xs)[None, :])[0].astype(np.float64) * ys + ym
+        if self.use_net:
+            dy = self.net.forward(((f - xm) / xs)[None, :])[0].astype(np.float64) * ys + ym
+        else:
+            dy = np.zeros_like(quad)
         a = coef[m - 1] + dS * (quad + dy)
         r = Phi.shape[1]
         cand = (mean + Phi @ torch.from_numpy(a[:r]).to(self.dev)).cpu().numpy()
