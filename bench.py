@@ -39,6 +39,7 @@ from __future__ import annotations
 
 import argparse
 import ctypes
+import faulthandler
 import json
 import os
 import statistics
@@ -673,6 +674,7 @@ def run_vefem(args):
 
 
 def main():
+    faulthandler.enable()   # a crash in native code still prints the Python stack
     args = parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -66,7 +66,8 @@ def test_singular_diagonal_factor_falls_back(monkeypatch):
     def splu(A, permc_spec=None, diag_pivot_thresh=None, **kw):
         if diag_pivot_thresh == 0.0:
             raise RuntimeError("Factor is exactly singular")
-        return real(A, permc_spec=permc_spec, diag_pivot_thresh=diag_pivot_thresh, **kw)
+        assert permc_spec == "COLAMD" and diag_pivot_thresh is None
+        return real(A, permc_spec=permc_spec, **kw)
     monkeypatch.setattr(LS.spla, "splu", splu)
     lu = LS.SparseLU(rp, ci, mesh).factor(v)
     assert lu.pivoted and lu.refactorisations == 1

@@ -11,8 +11,9 @@ about half the fill of SuperLU's column-AMD order.
 
 The factorisation takes diagonal pivots (diag_pivot_thresh 0, the order is
 fixed by the dissection); when a pivot is exactly zero, or the relative
-residual of a solve exceeds ``check_tol``, the matrix is refactorised with
-partial pivoting (and the solve repeated).
+residual of a solve exceeds ``check_tol``, the matrix is refactorised by
+SuperLU's default path (column AMD, threshold partial pivoting) and the
+solve repeated.
 """
 from __future__ import annotations
 
@@ -92,10 +93,15 @@ class SparseLU:
         try:
             self.lu = spla.splu(self.A, permc_spec="NATURAL", diag_pivot_thresh=0.0)
         except RuntimeError:        # an exactly zero diagonal pivot
-            self.lu = spla.splu(self.A, permc_spec="NATURAL", diag_pivot_thresh=1.0)
-            self.pivoted = True
-            self.refactorisations += 1
+            self._fallback()
         return self
+
+    def _fallback(self):
+        """SuperLU's own robust path: column AMD and threshold partial pivoting
+        (its defaults), on the same (dissection-ordered) matrix."""
+        self.lu = spla.splu(self.A, permc_spec="COLAMD")
+        self.pivoted = True
+        self.refactorisations += 1
 
     def solve(self, b: np.ndarray) -> np.ndarray:
         if self.perm is None:
@@ -106,9 +112,7 @@ class SparseLU:
             nb = np.linalg.norm(bp)
             r = np.linalg.norm(self.A @ xp - bp)
             if not np.isfinite(r) or r > self.check_tol * max(nb, 1e-300):
-                self.lu = spla.splu(self.A, permc_spec="NATURAL", diag_pivot_thresh=1.0)
-                self.pivoted = True
-                self.refactorisations += 1
+                self._fallback()
                 xp = self.lu.solve(bp)
         x = np.empty_like(xp)
         x[self.perm] = xp
