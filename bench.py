@@ -162,7 +162,10 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
-def dist_setup():
+def dist_setup(backend: str = "nccl"):
+    """torchrun environment: one process per GPU (replicas: each rank assembles
+    its own instance; the only collectives are the barrier and the max of the
+    timings).  backend "gloo" serves the CPU tests of this path."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -170,9 +173,26 @@ def dist_setup():
     if world > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
     return world, rank, local, dist
+
+
+def max_over_ranks(x: float, dist, device=None) -> float:
+    """The largest x over all ranks (the job's time is its slowest rank's)."""
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(world: int, units_per_rank: float, steps: int, seconds: float) -> float:
+    """Whole-job throughput of replicas: every rank processes units_per_rank per
+    step, the job time is the slowest rank's."""
+    return world * units_per_rank * steps / seconds
 
 
 def fp64_peak(device: int):
@@ -550,12 +570,8 @@ def run_vefem(args):
     if dist:
         dist.barrier()
     clk = clocks.stop()
-    ms = ev0.elapsed_time(ev1)
-    if dist:
-        tm = torch.tensor([ms], device=d)
-        dist.all_reduce(tm, op=dist.ReduceOp.MAX)
-        ms = float(tm.item())
-    value = world * nel * args.steps / (ms * 1e-3)
+    ms = max_over_ranks(ev0.elapsed_time(ev1), dist, d)
+    value = replica_rate(world, nel, args.steps, ms * 1e-3)
 
     # ---- residual-only ('MNR') on the same state
     rflags = V.VEFEM_RESIDUAL | V.VEFEM_ZERO_FIRST | V.VEFEM_TIMING
@@ -610,12 +626,8 @@ def run_vefem(args):
     t0 = time.perf_counter()
     for _ in range(args.steps):
         asm.assemble(hTL, hEU, eflags, hb, hv, on_device=False)
-    e2e_s = time.perf_counter() - t0
-    if dist:
-        te = torch.tensor([e2e_s], device=d)
-        dist.all_reduce(te, op=dist.ReduceOp.MAX)
-        e2e_s = float(te.item())
-    e2e = {"value": world * nel * args.steps / e2e_s, "unit": UNIT,
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist, d)
+    e2e = {"value": replica_rate(world, nel, args.steps, e2e_s), "unit": UNIT,
            "h2d_bytes_per_step": int(hTL.nbytes + hEU.nbytes),
            "d2h_bytes_per_step": int(hb.nbytes + hv.nbytes)}
 
