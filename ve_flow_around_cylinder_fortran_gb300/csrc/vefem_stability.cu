@@ -403,12 +403,13 @@ constexpr int ST_CH_OUT = ST_JCH * 900;                              // outputs 
 constexpr int ST_PER_T = (ST_CH_OUT + ST_THREADS - 1) / ST_THREADS;  // outputs per thread (11)
 constexpr int ST_A2 = ST_NQ + 1;                                     // row stride of A2
 
-// Shared memory: D [9][33][10][3] coefficient derivatives of one matrix, A2
-// [30][ST_A2] the test-side contraction of one Gauss point for one chunk of
-// three test nodes, and the base quantities of the 9 Gauss points.
+// Shared memory: D and DB [9][33][10][3] coefficient derivatives (A at one K
+// and, from the same evaluations at K = 0, B), A2 [30][ST_A2] the test-side
+// contraction of one Gauss point for one chunk of three test nodes, and the
+// base quantities of the 9 Gauss points.
 __host__ __device__ constexpr size_t st_smem_doubles()
 {
-    return (size_t)9 * ST_NQ * ST_NEQ * 3 + (size_t)ST_JCH * ST_NEQ * ST_A2;
+    return (size_t)2 * 9 * ST_NQ * ST_NEQ * 3 + (size_t)ST_JCH * ST_NEQ * ST_A2;
 }
 
 __global__ void __launch_bounds__(ST_THREADS)
@@ -416,7 +417,8 @@ k_stability(const StabArgs a, const KParams prm)
 {
     extern __shared__ __align__(16) double sm[];
     double *D = sm;                                   // [9][33][10][3]
-    double *A2 = D + 9 * ST_NQ * ST_NEQ * 3;          // [30][ST_A2]
+    double *DB = D + 9 * ST_NQ * ST_NEQ * 3;          // [9][33][10][3]
+    double *A2 = DB + 9 * ST_NQ * ST_NEQ * 3;         // [30][ST_A2]
     StabBase *base = reinterpret_cast<StabBase *>(A2 + ST_JCH * ST_NEQ * ST_A2);
     __shared__ double s_tlb[9 * ST_NEQ];
     __shared__ double s_dFx[9][9], s_dFy[9][9], s_lap[9][9], s_H2[9], s_W[9];
@@ -453,18 +455,25 @@ k_stability(const StabArgs a, const KParams prm)
         double *out = a.es + (size_t)e * 4 * ST_BLK;
         // element block m: 0 B (K = 0), 1 A(0), 2 A(+1), 3 A(-1); layout
         // ((jnod*9 + inod)*10 + jeq)*10 + ieq: row (jnod, jeq) = equation of test node
-        // jnod, column (inod, ieq) = unknown of trial node inod
+        // jnod, column (inod, ieq) = unknown of trial node inod.  The K = 0
+        // evaluations give both B and A(0).
         for (int m = 0; m < 4; m++) {
             const double K = m == 2 ? 1.0 : (m == 3 ? -1.0 : 0.0);
-            for (int w = t; w < 9 * ST_NQ; w += ST_THREADS) {
-                const int gp = w / ST_NQ, q = w % ST_NQ;
-                double ca[ST_NEQ][3], cb[ST_NEQ][3];
-                stab_coef(prm, base[gp], K, a.kz, q, ca, cb);
-                double *dst = D + (size_t)w * ST_NEQ * 3;
-                for (int e2 = 0; e2 < ST_NEQ; e2++)
-                    for (int c = 0; c < 3; c++) dst[e2 * 3 + c] = m == 0 ? cb[e2][c] : ca[e2][c];
+            if (m != 1) {
+                for (int w = t; w < 9 * ST_NQ; w += ST_THREADS) {
+                    const int gp = w / ST_NQ, q = w % ST_NQ;
+                    double ca[ST_NEQ][3], cb[ST_NEQ][3];
+                    stab_coef(prm, base[gp], K, a.kz, q, ca, cb);
+                    double *da = D + (size_t)w * ST_NEQ * 3, *db = DB + (size_t)w * ST_NEQ * 3;
+                    for (int e2 = 0; e2 < ST_NEQ; e2++)
+                        for (int c = 0; c < 3; c++) {
+                            da[e2 * 3 + c] = ca[e2][c];
+                            if (m == 0) db[e2 * 3 + c] = cb[e2][c];
+                        }
+                }
+                __syncthreads();
             }
-            __syncthreads();
+            const double *Dm = m == 0 ? DB : D;
             for (int j0 = 0; j0 < 9; j0 += ST_JCH) {
                 double acc[ST_PER_T];
 #pragma unroll
@@ -475,7 +484,7 @@ k_stability(const StabArgs a, const KParams prm)
                     for (int it = t; it < ST_JCH * ST_NEQ * ST_NQ; it += ST_THREADS) {
                         const int row = it / ST_NQ, q = it % ST_NQ;
                         const int jn = j0 + row / ST_NEQ, je = row % ST_NEQ;
-                        const double *dd = D + ((size_t)(gp * ST_NQ + q) * ST_NEQ + je) * 3;
+                        const double *dd = Dm + ((size_t)(gp * ST_NQ + q) * ST_NEQ + je) * 3;
                         A2[row * ST_A2 + q] = w * (s_bfn[gp][jn] * dd[0] + s_dFx[gp][jn] * dd[1]
                                                    + s_dFy[gp][jn] * dd[2]);
                     }
