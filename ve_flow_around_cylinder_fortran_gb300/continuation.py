@@ -150,6 +150,7 @@ class ArclengthContinuation:
         self.judge_s = 0.0
         self.cor0 = 1.0          # first correction norm of the last solve (cor_norm0_Main)
         self.have_lu = False     # a factorisation exists (LS%maxit > 0)
+        self.failed_factorisations = 0
 
     # state vector x = [TL in node-major order, lambda]
     def pack(self, TL, EU):
@@ -199,12 +200,29 @@ class ArclengthContinuation:
             self.lrow(x, b, vals)
             res_norm = float(np.linalg.norm(b))
             t1 = time.perf_counter()
+            if not np.isfinite(res_norm):
+                # a diverged iterate (non-finite residual): a failed solve
+                return x, it, nfac, res_norm, lu, False
             if want:
-                lu = self.solver.factor(vals)
+                try:
+                    lu = self.solver.factor(vals)
+                except RuntimeError:
+                    # a singular Jacobian (SuperLU: exactly zero pivot under
+                    # partial pivoting too) fails this solve like divergence;
+                    # the caller restarts with the relaxation halved
+                    self.failed_factorisations += 1
+                    self.have_lu = False
+                    tm["factor"] += time.perf_counter() - t1
+                    return x, it, nfac, res_norm, None, False
                 self.have_lu = True
                 nfac += 1
             t2 = time.perf_counter()
-            s = lu.solve(b)
+            try:
+                s = lu.solve(b)
+            except RuntimeError:     # its pivoted re-factorisation was singular
+                self.failed_factorisations += 1
+                self.have_lu = False
+                return x, it, nfac, res_norm, None, False
             t3 = time.perf_counter()
             tm["assembly"] += t1 - t0
             tm["factor"] += t2 - t1
