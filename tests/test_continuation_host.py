@@ -1,0 +1,86 @@
+"""Host logic of the arclength driver on the oracle assembly (no GPU): a
+Newton step whose Jacobian cannot be factorised (SuperLU: exactly singular)
+or whose residual is not finite fails that solve, and the emergency restart
+(relaxation halved, emergencyNewtonRaphson) converges to the same point."""
+import types
+
+import numpy as np
+import pytest
+
+from oracle_assembly import OracleAssembly
+from ve_flow_around_cylinder_fortran_gb300 import continuation as C
+from ve_flow_around_cylinder_fortran_gb300 import mesh as M
+from ve_flow_around_cylinder_fortran_gb300 import newton as N
+from ve_flow_around_cylinder_fortran_gb300 import pattern as P
+from ve_flow_around_cylinder_fortran_gb300 import state as S
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _oracle():
+    from oracle import oracle as O
+    O.build()
+
+
+def _driver(max_steps=2):
+    phys = S.oldroyd_b(0.1, 0.59, "SQRT", nex=1)
+    mesh = M.build_cylinder_mesh(40, exact=False)
+    TL, EU = N.initial_state(mesh, phys)
+    rowptr, colind = P.build_pattern(mesh.element_nodes(), mesh.nnodes, phys.nex)
+    rows, values = N.boundary_conditions(mesh, phys)
+    asm = types.SimpleNamespace(rowptr=rowptr, colind=colind, N=len(rowptr) - 1,
+                                nnodes=mesh.nnodes)
+    oa = OracleAssembly(phys, mesh, rowptr, colind, rows, values)
+    cfg = C.ArclengthSettings(dArN=0.01, max_steps=max_steps)
+    return C.ArclengthContinuation(asm, mesh, phys, "fd64", cfg, assembly=oa), TL, EU
+
+
+def test_singular_factorisation_restarts_newton():
+    ref, TL, EU = _driver()
+    r0, x0 = ref.run(TL, EU)
+    cont, TL, EU = _driver()
+    orig = cont.solver.factor
+    calls = {"n": 0}
+
+    def factor(vals):
+        calls["n"] += 1
+        if calls["n"] == 2:
+            raise RuntimeError("Factor is exactly singular")
+        return orig(vals)
+
+    cont.solver.factor = factor
+    r1, x1 = cont.run(TL, EU)
+    assert cont.failed_factorisations == 1
+    assert r1[0].emergencies == 1 and r0[0].emergencies == 0
+    for a, b in zip(x0, x1):
+        assert np.max(np.abs(a - b)) <= 1e-8 * np.max(np.abs(a))
+    assert all(r.res_norm < 1e-10 for r in r1)
+
+
+def test_non_finite_residual_restarts_newton():
+    cont, TL, EU = _driver(max_steps=1)
+    orig = cont.dev
+    calls = {"n": 0}
+
+    def assemble(TL_, EU_, want):
+        calls["n"] += 1
+        b, v = orig(TL_, EU_, want)
+        if calls["n"] == 2:
+            b[0] = np.nan
+        return b, v
+
+    cont.dev = assemble
+    cont.dev.set_values = orig.set_values
+    r, x = cont.run(TL, EU)
+    assert r[0].emergencies == 1 and r[0].res_norm < 1e-10
+
+
+def test_persistent_singularity_stops_with_an_error():
+    cont, TL, EU = _driver(max_steps=1)
+
+    def factor(vals):
+        raise RuntimeError("Factor is exactly singular")
+
+    cont.solver.factor = factor
+    with pytest.raises(RuntimeError, match="Newton failed at increment 1"):
+        cont.run(TL, EU)
+    assert cont.failed_factorisations == 7       # xF = 1, 1/2, ..., 1/64
