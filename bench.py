@@ -75,6 +75,8 @@ def parse_args():
     ap.add_argument("--cont-nel", type=int, default=500,
                     help="mesh of the continuation comparison (0 = skip it)")
     ap.add_argument("--cont-wi", type=float, default=1.0, help="Wi the continuation ends at")
+    ap.add_argument("--cont-log", action="store_true",
+                    help="with --continuation-only: every Newton iteration and step on stderr")
     ap.add_argument("--no-secant", action="store_true",
                     help="leave out the secant-predictor arm of the continuation comparison")
     ap.add_argument("--continuation-only", action="store_true",
@@ -283,14 +285,15 @@ def run_reference(args):
 
 
 def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=None,
-                         secant: bool = True):
+                         secant: bool = True, step_log=None):
     """Arclength continuation Wi 0.1 -> wi_end (Oldroyd-B, beta = 0.59, SQRT
     form) on the GPU assembly, arms from the same start: the plain FP64 path
     (FD64 Jacobian, the reference's tangent predictor), the same with a
     secant predictor, the learned + mixed path (FP32 exact Jacobian with FP64
-    residual, learned POD/MLP predictor trained online after the first 20
-    points), and the same without the network (its reduced-space quadratic
-    extrapolation alone: the ablation).  Every point is converged to
+    residual, learned POD/MLP predictor: cubic extrapolation in the POD space
+    of the converged points from the 4th point on, corrected by the network
+    trained online after the first 20 points), and the same without the
+    network (the reduced-space extrapolation alone: the ablation).  Every point is converged to
     ||R|| < 1e-10 and ||dx|| < 1e-10; host wall time per arm."""
     from ve_flow_around_cylinder_fortran_gb300 import continuation as C
     from ve_flow_around_cylinder_fortran_gb300 import learned as LP
@@ -303,11 +306,13 @@ def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=Non
     cfg = C.ArclengthSettings(dArN=0.01, lam_max=wi_end / phys.Wi0, max_steps=2000)
     arms, states = {}, {}
     runs = [("plain_fp64", "fd64", None), ("learned_fp32", "exact32", "learned"),
-            ("pod_quadratic_fp32", "exact32", "ablate")]
+            ("pod_cubic_fp32", "exact32", "ablate")]
     if secant:
         runs.insert(1, ("secant_fp64", "fd64", "secant"))
     for name, jac, kind in runs:
-        cont = C.ArclengthContinuation(asm, mesh, phys, jac, cfg)
+        cont = C.ArclengthContinuation(asm, mesh, phys, jac, cfg, log=step_log)
+        if step_log:
+            step_log(f"arm {name}")
         pred = None
         if kind in ("learned", "ablate"):
             pred = LP.LearnedPredictor(n_modes=32, start=20, device=f"cuda:{device}",
@@ -323,14 +328,16 @@ def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=Non
         arms[name] = {
             "jacobian": jac,
             "predictor": {"learned": "learned POD/MLP", "secant": "secant", None: "tangent",
-                          "ablate": "POD quadratic extrapolation, network off"}[kind],
+                          "ablate": "POD cubic extrapolation, network off"}[kind],
             "wall_s": wall, "steps": len(recs), "steps_per_s": len(recs) / wall,
             "newton_iterations": sum(r.newton_iterations for r in recs),
             "factorisations": sum(r.factorisations for r in recs),
             "learned_taken": sum(r.predictor == "learned" for r in recs),
+            "extrapolation_taken": sum(r.predictor == "extrapolation" for r in recs),
             "mean_err_pr_after_20": float(np.mean([r.pred_error for r in recs[20:]]))
             if len(recs) > 20 else None,
             "emergency_restarts": sum(r.emergencies for r in recs),
+            "singular_factorisations": cont.failed_factorisations,
             "final_wi": recs[-1].wi, "max_final_res_norm": max(r.res_norm for r in recs),
             "time_split_s": {"assembly": sum(r.assembly_s for r in recs),
                              "lu_factor": sum(r.factor_s for r in recs),
@@ -347,7 +354,7 @@ def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=Non
     xp = states["plain_fp64"]
     lp = np.array([x[-1] for x in xp])
     dev = 0.0
-    for x in states["learned_fp32"][20:-1]:
+    for x in states["learned_fp32"][1:-1]:
         k = int(np.searchsorted(lp, x[-1]))
         if 0 < k < len(lp):
             w = (x[-1] - lp[k - 1]) / (lp[k] - lp[k - 1])
@@ -527,8 +534,9 @@ def run_vefem(args):
         return 0
     if args.continuation_only:
         if rank == 0:
-            out = continuation_compare(args.cont_nel, args.cont_wi, dev,
-                                       secant=not args.no_secant)
+            out = continuation_compare(
+                args.cont_nel, args.cont_wi, dev, secant=not args.no_secant,
+                step_log=(lambda m: print(m, file=sys.stderr, flush=True)) if args.cont_log else None)
             print(json.dumps({"continuation": out}))
         if dist:
             dist.destroy_process_group()

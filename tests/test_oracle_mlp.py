@@ -137,3 +137,38 @@ def test_learned_prediction_beats_tangent_on_smooth_branch():
     cand = pred.predict(25, x1, t, dS, x_plain)
     assert pred.trainings == 5
     assert np.linalg.norm(cand - truth) < 0.2 * np.linalg.norm(x_plain - truth)
+
+
+def test_trained_network_gains_over_extrapolation_alone():
+    """What the network adds: on a smooth branch walked with the arclength
+    plane, predictions of the next six points by the cubic extrapolation in
+    the POD space with the trained network's correction are on average
+    closer to the corrected points than the extrapolation alone (both
+    candidates of the same predictor, the network retrained after each
+    point)."""
+    pytest.importorskip("torch")
+    from scipy.optimize import brentq
+
+    from ve_flow_around_cylinder_fortran_gb300 import learned as LP
+    for h in (0.08, 0.12):
+        curve = _Curve()
+        ref = MLPRef(2 + 3 * 8, 8, width=64, hidden=3)
+        ref.init_params(0)
+        pred = LP.LearnedPredictor(n_modes=8, start=20, net=ref, device="cpu", iters=300,
+                                   lr=1e-3, order=3)
+        ss = list(np.cumsum(np.full(22, h)))
+        _feed(pred, curve, ss)
+        err = {"learned": [], "extrapolation": []}
+        for k in range(23, 29):
+            x1, x0 = curve(ss[-1]), curve(ss[-2])
+            dS = np.linalg.norm(x1 - x0)
+            t = (x1 - x0) / dS
+            s_star = brentq(lambda s: t @ (curve(s) - x1) - dS, ss[-1], ss[-1] + 5 * h)
+            truth = curve(s_star)
+            cands = dict(pred.candidates(k, x1, t, dS, x1 + t * dS))
+            assert set(cands) == {"learned", "extrapolation"}
+            for name, x in cands.items():
+                err[name].append(np.linalg.norm(x - truth) / np.linalg.norm(truth))
+            ss.append(s_star)
+            pred.observe(k, truth, 0.1 + 0.05 * s_star)
+        assert np.mean(err["learned"]) < 0.7 * np.mean(err["extrapolation"]), (h, err)

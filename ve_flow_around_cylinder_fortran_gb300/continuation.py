@@ -264,11 +264,16 @@ class ArclengthContinuation:
             pred_name = "plain"
             if predictor is not None and k > 2:
                 tp = time.perf_counter()
-                cand = predictor.predict(k, x_o, t, dS, x_p)
-                if cand is not None and getattr(predictor, "replaces", False):
-                    x_p, pred_name = cand, type(predictor).__name__
-                elif cand is not None:
-                    x_p, pred_name = self._judge(x_p, cand)
+                if hasattr(predictor, "candidates"):
+                    cands = predictor.candidates(k, x_o, t, dS, x_p)
+                    if cands:
+                        x_p, pred_name = self._judge([("plain", x_p)] + cands)
+                else:
+                    cand = predictor.predict(k, x_o, t, dS, x_p)
+                    if cand is not None and getattr(predictor, "replaces", False):
+                        x_p, pred_name = cand, type(predictor).__name__
+                    elif cand is not None:
+                        x_p, pred_name = self._judge([("plain", x_p), ("learned", cand)])
                 self.timers["predictor"] += time.perf_counter() - tp
             # emergencyNewtonRaphson (Newton_Raphson_mod.F90:533-584): restart
             # from the prediction with the relaxation halved, 50 x Niter
@@ -341,18 +346,20 @@ class ArclengthContinuation:
             x_p = x.copy() if t is None else x + t * dS
         return records, states
 
-    def _judge(self, x_plain, x_cand):
-        """Newton judges the learned prediction by residual norm: the candidate
-        is used only when its residual is smaller than the plain prediction's."""
+    def _judge(self, cands):
+        """Newton judges the predictions by residual norm: of the (name, x)
+        candidates, the plain prediction first, the one with the smallest
+        residual (Dirichlet and lambda rows included) is taken; ties keep
+        the earlier one."""
         t0 = time.perf_counter()
-        r = []
-        for x in (x_plain, x_cand):
+        best, best_r = cands[0], None
+        for name, x in cands:
             TL, EU = self.unpack(x)
             self._update_inflow(float(EU[0]))
             b, _ = self.dev(TL, EU, False)
             self.lrow(x, b, None)
-            r.append(float(np.linalg.norm(b)))
+            r = float(np.linalg.norm(b))
+            if best_r is None or r < best_r:
+                best, best_r = (name, x), r
         self.judge_s += time.perf_counter() - t0
-        if r[1] < r[0]:
-            return x_cand, "learned"
-        return x_plain, "plain"
+        return best[1], best[0]

@@ -15,23 +15,26 @@ This module adds a learned prediction in a reduced space:
   Wi_{j-1}, the arclength step ds_j = s_j - s_{j-1}, the last coefficient
   vector a_{j-1} and the two last slopes (a_{j-1} - a_{j-2}) / ds_{j-1},
   (a_{j-2} - a_{j-3}) / ds_{j-2} (the last three coefficient vectors in
-  difference form).  Output: the change of slope
-  (a_j - a_{j-1}) / ds_j - (a_{j-1} - a_{j-2}) / ds_{j-1}; an output of zero is
-  the secant predictor in the reduced space.  Inputs and outputs are
-  standardised over the training set.
-* Online training: once ``start`` points have converged, the basis is
-  rebuilt and the network retrained (warm start) on all samples after every
-  converged point.
-* Prediction: a = a_m + dS (quad + net(...)) with quad the quadratic
-  extrapolation of the slopes, and the candidate x = mean + Phi a.  The
+  difference form).  Output: the slope (a_j - a_{j-1}) / ds_j minus the
+  slope of the polynomial extrapolation in s through the last ``order`` + 1
+  points (cubic by default); an output of zero is that extrapolation.  Inputs
+  and outputs are standardised over the training set.
+* Online training: once ``start`` points have converged (20), the network is
+  trained, and retrained (warm start) on all samples after every converged
+  point; the basis is rebuilt after every point from ``predict_from`` (4) on.
+* Prediction: a = a_m + dS (poly + net(...)) with poly the extrapolated
+  slope (the network term only once it is trained), and the candidate
+  x = mean + Phi a.  The
   candidate does not use the tangent: the tangent is solved with the last
   factorised Jacobian, taken at the first Newton iterate rather than at the
   converged point, and most of the tangent step's error lies outside the
   span of the converged snapshots.
 
-Newton stays the corrector and the judge: the continuation takes the
-candidate only when its residual norm is below the tangent prediction's
-(ArclengthContinuation._judge).
+Newton stays the corrector and the judge: of the tangent prediction, the
+extrapolation and the network-corrected extrapolation the continuation
+takes the one of the smallest residual norm (ArclengthContinuation._judge),
+so an untrained or mistaken network costs one residual evaluation and
+never a worse starting point.
 """
 from __future__ import annotations
 
@@ -43,11 +46,20 @@ import numpy as np
 class LearnedPredictor:
     def __init__(self, n_modes: int = 32, start: int = 20, width: int = 256, hidden: int = 3,
                  iters: int = 400, lr: float = 1.0e-3, seed: int = 0, device: str = "cuda:0",
-                 net=None, log=None, use_net: bool = True):
+                 net=None, log=None, use_net: bool = True, order: int = 3,
+                 predict_from: int | None = 4):
         import torch
         self.torch = torch
         self.dev = torch.device(device)
+        # the network trains once ``start`` points have converged; the
+        # reduced-space extrapolation predicts from ``predict_from`` points on
+        # (by default from ``start``), with the network's correction added
+        # once it is trained
         self.n_modes, self.start = n_modes, start
+        self.predict_from = start if predict_from is None else predict_from
+        if self.predict_from < 4:
+            raise ValueError("the reduced extrapolation needs 4 converged points")
+        self.trained = False
         self.iters, self.lr = iters, lr
         self.in_dim = 2 + 3 * n_modes
         if net is None:
@@ -68,6 +80,11 @@ class LearnedPredictor:
         # use_net = False: the ablation without the network (the reduced-space
         # quadratic extrapolation alone)
         self.use_net = use_net
+        # degree of the polynomial extrapolation in s the network corrects
+        # (3: the cubic through the last four points)
+        if order < 1:
+            raise ValueError("extrapolation order must be >= 1")
+        self.order = order
 
     # ---- data --------------------------------------------------------------
     def observe(self, k: int, x: np.ndarray, wi: float):
@@ -76,7 +93,7 @@ class LearnedPredictor:
             self.s.append(self.s[-1] + float(self.torch.linalg.vector_norm(t - self.X[-1])))
         self.X.append(t)
         self.wi.append(float(wi))
-        if len(self.X) >= self.start:
+        if len(self.X) >= min(self.start, self.predict_from):
             self._fit()
 
     def _pod(self):
@@ -117,13 +134,27 @@ class LearnedPredictor:
         ds2 = self.s[j - 2] - self.s[j - 3]
         sl1 = (coef[j - 1] - coef[j - 2]) / ds1
         sl2 = (coef[j - 2] - coef[j - 3]) / ds2
-        # slopes are derivatives at interval midpoints: exact for a quadratic a(s)
-        quad = sl1 + (sl1 - sl2) * (ds_j + ds1) / (ds1 + ds2)
+        q = min(self.order, j - 1)
+        if q == 2:
+            # slopes are derivatives at interval midpoints: exact for a quadratic a(s)
+            quad = sl1 + (sl1 - sl2) * (ds_j + ds1) / (ds1 + ds2)
+        else:
+            # Lagrange extrapolation through the last q + 1 points
+            sn = self.s[j - 1] + ds_j
+            nodes = self.s[j - 1 - q:j]
+            ext = np.zeros_like(coef[0])
+            for i in range(q + 1):
+                w = 1.0
+                for l in range(q + 1):
+                    if l != i:
+                        w *= (sn - nodes[l]) / (nodes[i] - nodes[l])
+                ext = ext + w * coef[j - 1 - q + i]
+            quad = (ext - coef[j - 1]) / ds_j
         return np.concatenate([[self.wi[j - 1], ds_j], coef[j - 1], sl1, sl2]), quad
 
     def _dataset(self, coef):
         X, Y = [], []
-        for j in range(3, len(self.X)):
+        for j in range(max(3, self.order + 1), len(self.X)):
             ds = self.s[j] - self.s[j - 1]
             f, quad = self._features(j, ds, coef)
             X.append(f)
@@ -134,40 +165,54 @@ class LearnedPredictor:
         t0 = time.perf_counter()
         mean, Phi, coef = self._pod()
         self.basis, self.coef = (mean, Phi), coef
-        X, Y = self._dataset(coef)
         t1 = time.perf_counter()
-        xm, xs = X.mean(axis=0), X.std(axis=0)
-        ym, ys = Y.mean(axis=0), Y.std(axis=0)
-        xs = np.where(xs > 1e-12 * max(1.0, np.abs(xm).max()), xs, 1.0)
-        ys = np.where(ys > 1e-30, ys, 1.0)
-        self.norm = (xm, xs, ym, ys)
-        if self.use_net:
+        if self.use_net and len(self.X) >= self.start:
+            X, Y = self._dataset(coef)
+            xm, xs = X.mean(axis=0), X.std(axis=0)
+            ym, ys = Y.mean(axis=0), Y.std(axis=0)
+            xs = np.where(xs > 1e-12 * max(1.0, np.abs(xm).max()), xs, 1.0)
+            ys = np.where(ys > 1e-30, ys, 1.0)
+            self.norm = (xm, xs, ym, ys)
             self.net.reset_optimizer()
             self.last_loss = self.net.train((X - xm) / xs, (Y - ym) / ys, self.iters, self.lr)
-        self.trainings += 1
+            self.trained = True
+            self.trainings += 1
+            if self.log:
+                self.log(f"learned predictor: {len(self.X)} snapshots, {Phi.shape[1]} modes, "
+                         f"training loss {self.last_loss:.3e}")
         self.timers["pod"] += t1 - t0
         self.timers["train"] += time.perf_counter() - t1
-        if self.log:
-            self.log(f"learned predictor: {len(self.X)} snapshots, {Phi.shape[1]} modes, "
-                     f"training loss {self.last_loss:.3e}")
 
     # ---- prediction --------------------------------------------------------
-    def predict(self, k: int, x_o: np.ndarray, t: np.ndarray, dS: float, x_plain: np.ndarray):
-        if self.basis is None or len(self.X) < self.start:
-            return None
+    def candidates(self, k: int, x_o: np.ndarray, t: np.ndarray, dS: float,
+                   x_plain: np.ndarray):
+        """The reduced-space candidates for the next point, best first:
+        [("learned", extrapolation + network)] once the network is trained,
+        then ("extrapolation", the polynomial extrapolation alone); empty
+        before ``predict_from`` points have converged."""
+        if self.basis is None or len(self.X) < self.predict_from:
+            return []
         t0 = time.perf_counter()
         torch = self.torch
         mean, Phi = self.basis
         m = len(self.X)
         coef = self.coef
-        f, quad = self._features(m, dS, coef)
-        xm, xs, ym, ys = self.norm
-        if self.use_net:
-            dy = self.net.forward(((f - xm) / xs)[None, :])[0].astype(np.float64) * ys + ym
-        else:
-            dy = np.zeros_like(quad)
-        a = coef[m - 1] + dS * (quad + dy)
         r = Phi.shape[1]
-        cand = (mean + Phi @ torch.from_numpy(a[:r]).to(self.dev)).cpu().numpy()
+        f, poly = self._features(m, dS, coef)
+        steps = []
+        if self.trained:
+            xm, xs, ym, ys = self.norm
+            dy = self.net.forward(((f - xm) / xs)[None, :])[0].astype(np.float64) * ys + ym
+            steps.append(("learned", poly + dy))
+        steps.append(("extrapolation", poly))
+        out = []
+        for name, slope in steps:
+            a = coef[m - 1] + dS * slope
+            out.append((name, (mean + Phi @ torch.from_numpy(a[:r]).to(self.dev)).cpu().numpy()))
         self.timers["predict"] += time.perf_counter() - t0
-        return cand
+        return out
+
+    def predict(self, k: int, x_o: np.ndarray, t: np.ndarray, dS: float, x_plain: np.ndarray):
+        """The first candidate (the network-corrected one once trained), or None."""
+        c = self.candidates(k, x_o, t, dS, x_plain)
+        return c[0][1] if c else None
