@@ -48,8 +48,9 @@ struct vefem_batch {
     int device = 0, ninst = 0, form = 0, spec = 0, nex = 0;
     int sms = 0;
     std::vector<vefem_ctx *> ctx;
-    cudaStream_t s = nullptr;
+    cudaStream_t s = nullptr, s2 = nullptr;   // s2: the FP64 residual beside the exact Jacobian
     cudaEvent_t ev[4] = {};
+    cudaEvent_t fork = nullptr, join = nullptr;
     float timing[3] = {0, 0, 0};
     int launches = 0;
     int64_t replays = 0;
@@ -155,9 +156,18 @@ void launch_all(vefem_batch *bt, int flags, bool timing, cudaError_t *err)
     if (timing && e == cudaSuccess) e = cudaEventRecord(bt->ev[1], s);
     const int res_grid = bt->sms * std::max(1, residual_batched_ctas_per_sm(bt->form));
     const int ex_grid = bt->sms * std::max(1, exact_batched_ctas_per_sm((int)vsize, bt->form, bt->spec));
+    const bool side = want_res && jmode;
     if (want_res && e == cudaSuccess) {
-        e = launch_residual64_batched(bt->d_inst, bt->d_res_work, bt->n_res_work, bt->form,
-                                      std::min(res_grid, bt->n_res_work), s);
+        cudaStream_t rs = s;
+        if (side) {
+            e = cudaEventRecord(bt->fork, s);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(bt->s2, bt->fork, 0);
+            rs = bt->s2;
+        }
+        if (e == cudaSuccess)
+            e = launch_residual64_batched(bt->d_inst, bt->d_res_work, bt->n_res_work, bt->form,
+                                          std::min(res_grid, bt->n_res_work), rs);
+        if (side && e == cudaSuccess) e = cudaEventRecord(bt->join, bt->s2);
         bt->launches++;
     }
     if (jmode && e == cudaSuccess) {
@@ -168,6 +178,7 @@ void launch_all(vefem_batch *bt, int flags, bool timing, cudaError_t *err)
                                                bt->spec, g, s);
         bt->launches++;
     }
+    if (side && e == cudaSuccess) e = cudaStreamWaitEvent(s, bt->join, 0);
     if (timing && e == cudaSuccess) e = cudaEventRecord(bt->ev[2], s);
     // scatter: the single-mesh element-ordered gathers, one launch per instance and
     // array (graph nodes), with each instance's tables as kernel arguments
@@ -234,6 +245,9 @@ extern "C" int vefem_batch_create(int ninst, const vefem_mesh *meshes, const vef
         BCK(cudaSetDevice(bt->device));
         BCK(cudaDeviceGetAttribute(&bt->sms, cudaDevAttrMultiProcessorCount, bt->device));
         BCK(cudaStreamCreateWithFlags(&bt->s, cudaStreamNonBlocking));
+        BCK(cudaStreamCreateWithFlags(&bt->s2, cudaStreamNonBlocking));
+        BCK(cudaEventCreateWithFlags(&bt->fork, cudaEventDisableTiming));
+        BCK(cudaEventCreateWithFlags(&bt->join, cudaEventDisableTiming));
         for (auto &ev : bt->ev) BCK(cudaEventCreate(&ev));
         for (int i = 0; i < ninst; i++) bt->total_el += bt->ctx[i]->nel;
         BCK(cudaMalloc(&bt->d_inst, ninst * sizeof(BatchInst)));
@@ -566,6 +580,10 @@ extern "C" int vefem_batch_destroy(vefem_batch *bt)
     for (void *q : bt->st_vals) cudaFree(q);
     for (auto &ev : bt->ev)
         if (ev) cudaEventDestroy(ev);
+    if (bt->s2) cudaStreamSynchronize(bt->s2);
+    if (bt->fork) cudaEventDestroy(bt->fork);
+    if (bt->join) cudaEventDestroy(bt->join);
+    if (bt->s2) cudaStreamDestroy(bt->s2);
     if (bt->s) cudaStreamDestroy(bt->s);
     delete bt;
     return VEFEM_OK;

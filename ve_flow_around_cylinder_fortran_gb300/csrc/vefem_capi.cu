@@ -388,6 +388,9 @@ extern "C" int vefem_create(const vefem_mesh *mesh, const vefem_csr *pat,
 
     cudaError_t ce = cudaSetDevice(ctx->device);
     if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking);
+    if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming);
+    if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&ctx->join, cudaEventDisableTiming);
     if (ce != cudaSuccess) {
         std::string m = std::string("cudaStreamCreate: ") + cudaGetErrorString(ce);
         delete ctx;
@@ -545,8 +548,19 @@ extern "C" int vefem_assemble(vefem_ctx *ctx, const double *TL, const double *EU
         CK(launch_fd64(ea, ctx->prm, s));
         ctx->launches++;
     } else {
+        // The FP64 residual and an exact Jacobian are independent until the
+        // scatter: the residual runs on a second stream, so the FP64 pipe works
+        // on it while the exact kernel keeps the FP32 pipes busy.
+        const bool side = want_res && want_jac;
         if (want_res) {
-            CK(launch_residual64(ea, ctx->prm, s));
+            if (side) {
+                CK(cudaEventRecord(ctx->fork, s));
+                CK(cudaStreamWaitEvent(ctx->stream2, ctx->fork, 0));
+                CK(launch_residual64(ea, ctx->prm, ctx->stream2));
+                CK(cudaEventRecord(ctx->join, ctx->stream2));
+            } else {
+                CK(launch_residual64(ea, ctx->prm, s));
+            }
             ctx->launches++;
         }
         if (jmode == VEFEM_JAC_EXACT64 || jac32) {
@@ -573,6 +587,7 @@ extern "C" int vefem_assemble(vefem_ctx *ctx, const double *TL, const double *EU
                 CK(launch_exact_batched<double>(ctx->d_self, ctx->d_work, (int)nel, ctx->prm.form, spec, grid, s));
             ctx->launches++;
         }
+        if (side) CK(cudaStreamWaitEvent(s, ctx->join, 0));
     }
     if (timing) CK(cudaEventRecord(ctx->ev[2], s));
 
@@ -730,6 +745,10 @@ extern "C" int vefem_destroy(vefem_ctx *ctx)
         if (p) cudaFree(p);
     for (int i = 0; i < 8; i++)
         if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+    if (ctx->stream2) cudaStreamSynchronize(ctx->stream2);
+    if (ctx->fork) cudaEventDestroy(ctx->fork);
+    if (ctx->join) cudaEventDestroy(ctx->join);
+    if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return VEFEM_OK;

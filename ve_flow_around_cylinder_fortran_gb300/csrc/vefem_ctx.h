@@ -17,6 +17,8 @@ struct vefem_ctx {
     int nedge = 0;
     vefem::KParams prm{};
     cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr;          // FP64 residual beside an exact Jacobian
+    cudaEvent_t fork = nullptr, join = nullptr;
     cudaEvent_t ev[8] = {};
     float timing[5] = {0, 0, 0, 0, 0};
     int launches = 0;
