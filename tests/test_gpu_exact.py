@@ -101,3 +101,29 @@ def test_exact_vs_fd_and_fp32_on_cylinder(form):
     big = np.abs(v64) > 1e-6 * scale
     rel = np.abs(v32[big] - v64[big]) / np.abs(v64[big])
     assert np.median(rel) < 1e-5
+
+
+@pytest.mark.parametrize("nel", [2000, 5000])
+def test_fp32_jacobian_finite_on_parallel_flow_start(nel):
+    """The continuation's starting state (fully developed channel flow with the
+    cylinder masked to rest) makes the constitutive residual C vanish up to
+    round-off over most of the channel; in FP32 the DCS magnitude
+    sqrt(0.5 C:C^T) then sees a negative argument at some Gauss points.  The
+    FP32 Jacobian stays finite there and within the FP32 tolerance of the
+    FD64 Jacobian."""
+    from ve_flow_around_cylinder_fortran_gb300 import newton as N
+    mesh = M.build_cylinder_mesh(nel)
+    phys = S.oldroyd_b(0.1, 0.59, "SQRT", nex=1)
+    TL, EU = N.initial_state(mesh, phys)
+    rowptr, colind = P.build_pattern(mesh.element_nodes(), mesh.nnodes, 1)
+    asm = V.BulkAssembler(mesh, phys, rowptr, colind, outlet_edges=True)
+    _, vfd = asm.set_equations_bulk(TL, EU, "NRP", jacobian="fd64", outlet_edges=True)
+    _, v32 = asm.set_equations_bulk(TL, EU, "NRP", jacobian="exact32", outlet_edges=True)
+    _, v64 = asm.set_equations_bulk(TL, EU, "NRP", jacobian="exact64", outlet_edges=True)
+    asm.close()
+    assert np.isfinite(v32).all() and np.isfinite(v64).all()
+    scale = np.max(np.abs(vfd))
+    # sqrt(0.5 C:C^T) has a kink at C = 0, where the forward difference and the
+    # derivative differ by O(|dC/dx|): a looser bound than on generic states
+    assert np.max(np.abs(v64 - vfd)) < 1e-4 * scale
+    assert np.max(np.abs(v32.astype(np.float64) - vfd)) < 1e-4 * scale

@@ -26,7 +26,6 @@ using namespace vefem;
 
 namespace {
 
-constexpr int RES_EPB = 8;                   // elements per residual work item (kernel block)
 const int EX_TILES[] = {1, 2, 4, 8};         // candidate element-batch tiles of the Jacobian kernel
 
 int size_class(int nel)

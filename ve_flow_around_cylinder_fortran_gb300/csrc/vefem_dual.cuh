@@ -1,7 +1,8 @@
 // Forward-mode dual number with one tangent direction, used to differentiate
 // the Gauss-point physics (vefem_physics.cuh) for the exact Jacobian.
 // sqrt and fabs take the derivative 0 at 0 (a subgradient), where the
-// classical derivative does not exist.
+// classical derivative does not exist; sqrt of a negative (round-off)
+// argument is 0 with derivative 0.
 #pragma once
 
 #include <math.h>
@@ -72,6 +73,13 @@ VD_SCALAR VD_HD Dual<T> operator/(U a, Dual<T> b)
 
 template <class T> VD_HD Dual<T> sqrt(Dual<T> a)
 {
+    // A negative argument is round-off of a quantity that is non-negative in
+    // the FP64 residual: the magnitude sqrt(0.5 C:C^T) of the constitutive
+    // residual C, which vanishes for an exact parallel-flow state, rounds
+    // below zero in FP32 when C12 and C21 are noise of opposite signs.  The
+    // Jacobian then takes value and derivative 0 (the subgradient at 0)
+    // instead of NaN; a NaN argument stays NaN.
+    if (a.v < (T)0) return Dual<T>((T)0, (T)0);
     const T r = sqrt(a.v);
     return Dual<T>(r, r > (T)0 ? a.d / (r + r) : (T)0);
 }

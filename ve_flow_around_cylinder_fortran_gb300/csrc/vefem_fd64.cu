@@ -238,8 +238,10 @@ __global__ void __launch_bounds__(FD_THREADS) k_fd64(const ElemArgs a, const KPa
 // ---------------------------------------------------------------------------
 // Residual-only kernel: thread = (element, Gauss point)
 
-constexpr int RS_EPB = 8;
-constexpr int RS_THREADS = RS_EPB * 9;   // 72
+// residual kernel: one thread per (element, Gauss point), RES_EPB elements per
+// CTA (vefem_internal.h)
+constexpr int RS_EPB = RES_EPB;
+constexpr int RS_THREADS = RS_EPB * 9;
 
 // elements [e0, e0 + count) of one mesh, count <= RS_EPB
 template <int FORM>

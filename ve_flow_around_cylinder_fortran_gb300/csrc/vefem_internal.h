@@ -11,6 +11,9 @@ namespace vefem {
 
 enum { FORM_T = 0, FORM_SQRT = 1 };
 
+// FP64 residual kernel: elements per CTA and per batched work item
+constexpr int RES_EPB = 8;
+
 // Specialisations that leave out terms which are exact zeros for the given
 // parameters; a sum that drops an exact-zero addend keeps its value, so the
 // results are the same as the general code (up to the sign of a zero result).
