@@ -39,6 +39,7 @@ from __future__ import annotations
 
 import argparse
 import ctypes
+import dataclasses
 import faulthandler
 import json
 import os
@@ -292,9 +293,12 @@ def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=Non
     secant predictor, the learned + mixed path (FP32 exact Jacobian with FP64
     residual, learned POD/MLP predictor: cubic extrapolation in the POD space
     of the converged points from the 4th point on, corrected by the network
-    trained online after the first 20 points), and the same without the
-    network (the reduced-space extrapolation alone: the ablation).  Every point is converged to
-    ||R|| < 1e-10 and ||dx|| < 1e-10; host wall time per arm."""
+    trained online after the first 20 points; factorisations reused across
+    steps while chord iterations contract), and two ablations: the learned
+    arm with the reference's factorisation-reuse rules, and the contraction
+    policy without the network (the reduced-space extrapolation alone).
+    Every point is converged to ||R|| < 1e-10 and ||dx|| < 1e-10; host wall
+    time per arm."""
     from ve_flow_around_cylinder_fortran_gb300 import continuation as C
     from ve_flow_around_cylinder_fortran_gb300 import learned as LP
     from ve_flow_around_cylinder_fortran_gb300 import newton as NW
@@ -304,19 +308,24 @@ def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=Non
     rowptr, colind = P.build_pattern(mesh.element_nodes(), mesh.nnodes, phys.nex)
     asm = V.BulkAssembler(mesh, phys, rowptr, colind, outlet_edges=True, device=device)
     cfg = C.ArclengthSettings(dArN=0.01, lam_max=wi_end / phys.Wi0, max_steps=2000)
+    # the learned + mixed arm reuses factorisations across steps while chord
+    # iterations contract (theta < 0.6); the plain arm keeps the reference's rules
+    chord = dataclasses.replace(cfg, reuse="contraction", theta_max=0.6)
     arms, states = {}, {}
-    runs = [("plain_fp64", "fd64", None), ("learned_fp32", "exact32", "learned"),
-            ("pod_cubic_fp32", "exact32", "ablate")]
+    runs = [("plain_fp64", "fd64", None, cfg), ("learned_fp32", "exact32", "learned", chord),
+            ("learned_fp32_reference_reuse", "exact32", "learned", cfg),
+            ("pod_cubic_fp32", "exact32", "ablate", chord)]
     if secant:
-        runs.insert(1, ("secant_fp64", "fd64", "secant"))
-    for name, jac, kind in runs:
-        cont = C.ArclengthContinuation(asm, mesh, phys, jac, cfg, log=step_log)
+        runs.insert(1, ("secant_fp64", "fd64", "secant", cfg))
+    for name, jac, kind, arm_cfg in runs:
+        cont = C.ArclengthContinuation(asm, mesh, phys, jac, arm_cfg, log=step_log)
         if step_log:
             step_log(f"arm {name}")
         pred = None
         if kind in ("learned", "ablate"):
             pred = LP.LearnedPredictor(n_modes=32, start=20, device=f"cuda:{device}",
                                        use_net=kind == "learned")
+            pred.warm_up(len(rowptr) - 1)      # one-time framework start-up, not timed
         elif kind == "secant":
             pred = C.SecantPredictor()
         t0 = time.perf_counter()
@@ -329,6 +338,8 @@ def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=Non
             "jacobian": jac,
             "predictor": {"learned": "learned POD/MLP", "secant": "secant", None: "tangent",
                           "ablate": "POD cubic extrapolation, network off"}[kind],
+            "factorisation_reuse": arm_cfg.reuse if arm_cfg.reuse == "reference"
+            else f"contraction (theta_max {arm_cfg.theta_max})",
             "wall_s": wall, "steps": len(recs), "steps_per_s": len(recs) / wall,
             "newton_iterations": sum(r.newton_iterations for r in recs),
             "factorisations": sum(r.factorisations for r in recs),

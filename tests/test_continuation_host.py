@@ -84,3 +84,61 @@ def test_persistent_singularity_stops_with_an_error():
     with pytest.raises(RuntimeError, match="Newton failed at increment 1"):
         cont.run(TL, EU)
     assert cont.failed_factorisations == 7       # xF = 1, 1/2, ..., 1/64
+
+
+def _branch_dev(xa, xb):
+    """Largest relative distance of the points xb from the branch through the
+    points xa (linear interpolation in lambda)."""
+    la = np.array([x[-1] for x in xa])
+    dev = 0.0
+    for x in xb[1:-1]:
+        k = int(np.searchsorted(la, x[-1]))
+        if 0 < k < len(la):
+            w = (x[-1] - la[k - 1]) / (la[k] - la[k - 1])
+            ref = (1 - w) * xa[k - 1] + w * xa[k]
+            dev = max(dev, float(np.linalg.norm(x - ref) / np.linalg.norm(ref)))
+    return dev
+
+
+def test_contraction_reuse_converges_on_the_same_branch_with_fewer_factorisations():
+    """The chord policy (factorisations kept across steps while the chord
+    iterations contract) converges every point to ||R|| < 1e-10 on the
+    branch of the reference policy, with the reduced-space predictor, and
+    factorises less often."""
+    from ve_flow_around_cylinder_fortran_gb300 import learned as LP
+    out = {}
+    for reuse in ("reference", "contraction"):
+        cont, TL, EU = _driver(max_steps=400)
+        cont.cfg = C.ArclengthSettings(dArN=0.01, max_steps=400, lam_max=6.0, reuse=reuse,
+                                       theta_max=0.6, factor_cost=30.0)
+        pred = LP.LearnedPredictor(n_modes=32, start=20, device="cpu", net=object(),
+                                   use_net=False)
+        recs, xs = cont.run(TL, EU, predictor=pred)
+        assert all(r.res_norm < 1e-10 for r in recs)
+        assert recs[-1].lam >= 6.0
+        out[reuse] = (sum(r.factorisations for r in recs), xs)
+    assert out["contraction"][0] < out["reference"][0]
+    # chord iterations converge to the same points as Newton: branch agreement
+    # limited by the linear interpolation between the reference points
+    assert _branch_dev(out["reference"][1], out["contraction"][1]) < 1e-3
+
+
+def test_contraction_reuse_far_start_takes_newton_steps():
+    """From the far initial state the chord policy takes full Newton steps
+    while the correction is above MNR_eps, as the reference does, and
+    converges the first point without an emergency restart."""
+    cont, TL, EU = _driver(max_steps=1)
+    cont.cfg = C.ArclengthSettings(dArN=0.01, max_steps=1, reuse="contraction", theta_max=0.6,
+                                   factor_cost=30.0)
+    recs, xs = cont.run(TL, EU)
+    ref, TL, EU = _driver(max_steps=1)
+    r0, x0 = ref.run(TL, EU)
+    assert recs[0].emergencies == 0 and recs[0].res_norm < 1e-10
+    assert np.max(np.abs(xs[0] - x0[0])) <= 1e-8 * np.max(np.abs(x0[0]))
+
+
+def test_unknown_reuse_policy_is_rejected():
+    cont, TL, EU = _driver(max_steps=1)
+    with pytest.raises(ValueError, match="reuse policy"):
+        C.ArclengthContinuation(cont.asm, cont.mesh, cont.phys, "fd64",
+                                C.ArclengthSettings(reuse="sometimes"), assembly=cont.dev)

@@ -25,7 +25,18 @@ Nex = 1 (the extra unknown lambda, Wi = Wi0 * lambda at every Gauss point):
   Niter iterations and dSo halved.
 
 A predictor object can replace the plain prediction (the learned POD/MLP
-predictor in ``learned.py``); Newton stays the corrector.  The host solves
+predictor in ``learned.py``); Newton stays the corrector.
+
+Factorisation reuse (``ArclengthSettings.reuse``): "reference" follows
+checkMNR and checkNewtonConvergence as above (every 10th iteration of a
+solve refactorises).  "contraction" is the policy of the learned + mixed
+path: the last factorisation is kept across steps for chord iterations as
+long as each one contracts the correction by theta_max or better and the
+iterations it predicts until the tolerance cost less than a factorisation;
+a stale factorisation that stops contracting is replaced at the iterate
+the failed chord step started from.  The residual, the tolerance and hence
+the converged points are the same; only the Jacobian the corrections are
+solved with is older.  The host solves
 with SuperLU in a nested-dissection order (linsolve.py, stand-in for
 MUMPS); the dense lambda row and the arclength column make the matrix
 bordered, and the lambda unknown is ordered last.
@@ -55,6 +66,16 @@ class ArclengthSettings:
     tol: float = 1.0e-10      # Newton tolerance on |s| and |R|
     lam_max: float = 10.0     # stop once lambda >= lam_max
     max_steps: int = 200
+    # factorisation reuse: "reference" (checkMNR / checkNewtonConvergence
+    # switching) or "contraction" (chord iterations on the last factorisation
+    # across steps, refactorised when their observed contraction makes the
+    # remaining iterations cost more than a new factorisation)
+    reuse: str = "reference"
+    # cost of a factorisation in chord iterations for "contraction"; None
+    # measures both costs online (host wall time)
+    factor_cost: float | None = None
+    chord_max: int = 30       # at most this many predicted chord iterations
+    theta_max: float = 1.0    # refactorise when a chord step contracts less than this
 
 
 @dataclasses.dataclass
@@ -151,6 +172,13 @@ class ArclengthContinuation:
         self.cor0 = 1.0          # first correction norm of the last solve (cor_norm0_Main)
         self.have_lu = False     # a factorisation exists (LS%maxit > 0)
         self.failed_factorisations = 0
+        if self.cfg.reuse not in ("reference", "contraction"):
+            raise ValueError(f"unknown factorisation reuse policy {self.cfg.reuse!r}")
+        # running costs (s) of a chord iteration and of a factorisation, for
+        # the "contraction" policy
+        self.t_iter = None
+        self.t_fac = None
+        self.reverted = 0        # chord steps undone because they did not contract
 
     # state vector x = [TL in node-major order, lambda]
     def pack(self, TL, EU):
@@ -170,10 +198,116 @@ class ArclengthContinuation:
         -- the factorisation of the previous solve -- when the first correction
         of the previous solve was below MNR_eps, except at every 100th
         increment (if that correction was above MNR_eps/10) and every 1000th."""
+        if self.cfg.reuse == "contraction":
+            return "MNR" if self.have_lu else "NRP"
         flag = "MNR" if self.cor0 < NW.MNR_EPS else "NRP"
         if (k % 100 == 0 and self.cor0 > NW.MNR_EPS / 10.0) or k % 1000 == 0:
             flag = "NRP"
         return flag if self.have_lu else "NRP"
+
+    def _factor_cost(self) -> float:
+        """A factorisation's cost in chord iterations."""
+        if self.cfg.factor_cost is not None:
+            return self.cfg.factor_cost
+        if self.t_iter is None or self.t_fac is None:
+            return 10.0
+        return self.t_fac / max(self.t_iter, 1e-9)
+
+    def _newton_chord(self, x0: np.ndarray, xF: float, max_iter: int, flag: str):
+        """Newton with the lambda row, reusing the last factorisation across
+        solves (chord iterations) while it contracts well enough.  With a
+        contraction rate theta = |s_k| / |s_(k-1)| observed on one
+        factorisation, finishing takes n = log(tol / |s_k|) / log(theta) more
+        iterations; a new factorisation is taken at the next iterate when n
+        exceeds ``chord_max`` or costs more than a factorisation plus three
+        iterations.  A chord step on an older factorisation that does not
+        contract (theta >= 1) is undone and the Jacobian assembled at the
+        iterate it started from; after a Newton step on a factorisation taken
+        at its own starting point the Jacobian is assembled at the new iterate
+        (the reference's 'MNR' -> 'NRP' switch).  Returns what _newton
+        returns."""
+        cfg = self.cfg
+        x = x0.copy()
+        tm = self.timers
+        res_norm = cor_new = 1.0
+        cor_old = None           # last correction on the current factorisation
+        x_prev = None            # the iterate that correction started from
+        prev_fresh = False       # the factorisation was taken at x_prev
+        lu = self.solver if self.have_lu else None
+        want = flag == "NRP" or lu is None
+        it = nfac = 0
+        while True:
+            if cor_new < cfg.tol and res_norm < cfg.tol:
+                return x, it, nfac, res_norm, lu, True
+            it += 1
+            t0 = time.perf_counter()
+            TL, EU = self.unpack(x)
+            self._update_inflow(float(EU[0]))
+            b, vals = self.dev(TL, EU, want)
+            self.lrow(x, b, vals)
+            res_norm = float(np.linalg.norm(b))
+            t1 = time.perf_counter()
+            if not np.isfinite(res_norm):
+                return x, it, nfac, res_norm, lu, False
+            if want:
+                try:
+                    lu = self.solver.factor(vals)
+                except RuntimeError:
+                    self.failed_factorisations += 1
+                    self.have_lu = False
+                    tm["factor"] += time.perf_counter() - t1
+                    return x, it, nfac, res_norm, None, False
+                self.have_lu = True
+                nfac += 1
+                cor_old = None
+            t2 = time.perf_counter()
+            try:
+                s = lu.solve(b)
+            except RuntimeError:
+                self.failed_factorisations += 1
+                self.have_lu = False
+                return x, it, nfac, res_norm, None, False
+            t3 = time.perf_counter()
+            tm["assembly"] += t1 - t0
+            tm["factor"] += t2 - t1
+            tm["solve"] += t3 - t2
+            if want:
+                c = (t1 - t0) + (t2 - t1)
+                self.t_fac = c if self.t_fac is None else 0.5 * (self.t_fac + c)
+            else:
+                c = (t1 - t0) + (t3 - t2)
+                self.t_iter = c if self.t_iter is None else 0.5 * (self.t_iter + c)
+            cor_new = float(np.linalg.norm(s))
+            if it == 1:
+                self.cor0 = cor_new
+            if self.log:
+                self.log(f"   {it:3d}. {'NRP' if want else 'MNR'}: RES_NORM = {res_norm:.4e}, "
+                         f"COR_NORM = {cor_new:.4e}")
+            if cor_new != cor_new or cor_new > NW.COR_NORM_DIV or it > max_iter:
+                return x, it, nfac, res_norm, lu, False
+            fresh = want
+            want = False
+            if cor_old is not None and cor_new >= cfg.tol:
+                theta = cor_new / cor_old
+                if theta >= 1.0 and not prev_fresh:
+                    # a stale factorisation that does not contract: undo the
+                    # chord step, refactorise where it started
+                    self.reverted += 1
+                    x = x_prev
+                    cor_new, want = cor_old, True
+                    continue
+                if theta >= cfg.theta_max:
+                    want = True
+                else:
+                    n = np.log(cfg.tol / cor_new) / np.log(theta)
+                    want = n > cfg.chord_max or n > self._factor_cost() + 3.0
+            elif fresh and cor_new > NW.MNR_EPS:
+                # far from the solution: full Newton steps, as the reference
+                # stays in 'NRP' until the correction drops below MNR_eps
+                want = True
+            cor_old = cor_new
+            x_prev, prev_fresh = x, fresh
+            x = x - xF * s
 
     def _newton(self, x0: np.ndarray, xF: float = 1.0, max_iter: int = NW.NITER,
                 flag: str = "NRP"):
@@ -181,6 +315,8 @@ class ArclengthContinuation:
         ``flag``; returns (x, iterations, factorisations, last residual norm,
         the solver holding the last factorisation, converged)."""
         cfg = self.cfg
+        if cfg.reuse == "contraction":
+            return self._newton_chord(x0, xF, max_iter, flag)
         x = x0.copy()
         tm = self.timers
         res_norm = cor_new = cor_old = 1.0
