@@ -80,6 +80,14 @@ def parse_args():
                     help="with --continuation-only: every Newton iteration and step on stderr")
     ap.add_argument("--no-secant", action="store_true",
                     help="leave out the secant-predictor arm of the continuation comparison")
+    ap.add_argument("--no-ablations", action="store_true",
+                    help="leave out the ablation arms of the continuation comparison")
+    ap.add_argument("--cont-arms", default="",
+                    help="comma-separated arm names of the continuation comparison to run "
+                         "(default: all)")
+    ap.add_argument("--newton-only", type=int, default=0, metavar="NEL",
+                    help="only the precision-form Newton comparison (FP64 vs FP32 Jacobian, "
+                         "natural continuation Wi 0.1, 0.3, 0.5) on a mesh of NEL quads")
     ap.add_argument("--continuation-only", action="store_true",
                     help="run only the continuation comparison and print its JSON line")
     ap.add_argument("--batch-inst", type=int, default=64,
@@ -286,7 +294,8 @@ def run_reference(args):
 
 
 def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=None,
-                         secant: bool = True, step_log=None):
+                         secant: bool = True, step_log=None, ablations: bool = True,
+                         only=None):
     """Arclength continuation Wi 0.1 -> wi_end (Oldroyd-B, beta = 0.59, SQRT
     form) on the GPU assembly, arms from the same start: the plain FP64 path
     (FD64 Jacobian, the reference's tangent predictor), the same with a
@@ -309,14 +318,19 @@ def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=Non
     asm = V.BulkAssembler(mesh, phys, rowptr, colind, outlet_edges=True, device=device)
     cfg = C.ArclengthSettings(dArN=0.01, lam_max=wi_end / phys.Wi0, max_steps=2000)
     # the learned + mixed arm reuses factorisations across steps while chord
-    # iterations contract (theta < 0.6); the plain arm keeps the reference's rules
-    chord = dataclasses.replace(cfg, reuse="contraction", theta_max=0.6)
+    # iterations contract (theta < 0.6) and cuts a failed step back (dS halved,
+    # predicted again) before relaxing; the plain arm keeps the reference's rules
+    chord = dataclasses.replace(cfg, reuse="contraction", theta_max=0.6, cutbacks=4)
     arms, states = {}, {}
     runs = [("plain_fp64", "fd64", None, cfg), ("learned_fp32", "exact32", "learned", chord),
             ("learned_fp32_reference_reuse", "exact32", "learned", cfg),
             ("pod_cubic_fp32", "exact32", "ablate", chord)]
     if secant:
         runs.insert(1, ("secant_fp64", "fd64", "secant", cfg))
+    if not ablations:
+        runs = [r for r in runs if r[0] not in ("learned_fp32_reference_reuse", "pod_cubic_fp32")]
+    if only:
+        runs = [r for r in runs if r[0] in only]
     for name, jac, kind, arm_cfg in runs:
         cont = C.ArclengthContinuation(asm, mesh, phys, jac, arm_cfg, log=step_log)
         if step_log:
@@ -339,7 +353,7 @@ def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=Non
             "predictor": {"learned": "learned POD/MLP", "secant": "secant", None: "tangent",
                           "ablate": "POD cubic extrapolation, network off"}[kind],
             "factorisation_reuse": arm_cfg.reuse if arm_cfg.reuse == "reference"
-            else f"contraction (theta_max {arm_cfg.theta_max})",
+            else f"contraction (theta_max {arm_cfg.theta_max}), {arm_cfg.cutbacks} step cutbacks",
             "wall_s": wall, "steps": len(recs), "steps_per_s": len(recs) / wall,
             "newton_iterations": sum(r.newton_iterations for r in recs),
             "factorisations": sum(r.factorisations for r in recs),
@@ -348,6 +362,7 @@ def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=Non
             "mean_err_pr_after_20": float(np.mean([r.pred_error for r in recs[20:]]))
             if len(recs) > 20 else None,
             "emergency_restarts": sum(r.emergencies for r in recs),
+            "step_cutbacks": sum(r.cutbacks for r in recs),
             "singular_factorisations": cont.failed_factorisations,
             "final_wi": recs[-1].wi, "max_final_res_norm": max(r.res_norm for r in recs),
             "time_split_s": {"assembly": sum(r.assembly_s for r in recs),
@@ -361,6 +376,14 @@ def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=Non
         if log:
             log(f"{name}: {arms[name]}")
     asm.close()
+    out = {
+        "workload": f"arclength continuation Wi 0.1 -> {wi_end}, Oldroyd-B beta=0.59, SQRT form, "
+                    f"{mesh.nel} Q2 quads ({len(rowptr) - 1} unknowns), LN0=1, dArN=0.01, "
+                    "Eps_Pr=1e-3, dS0=1, dS_max=50; host SuperLU (nested dissection) solve",
+        "arms": arms,
+    }
+    if "plain_fp64" not in states or "learned_fp32" not in states:
+        return out
     # the learned arm's points against the plain arm's branch (linear interpolation in lambda)
     xp = states["plain_fp64"]
     lp = np.array([x[-1] for x in xp])
@@ -371,15 +394,53 @@ def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=Non
             w = (x[-1] - lp[k - 1]) / (lp[k] - lp[k - 1])
             ref = (1 - w) * xp[k - 1] + w * xp[k]
             dev = max(dev, float(np.linalg.norm(x - ref) / np.linalg.norm(ref)))
-    return {
-        "workload": f"arclength continuation Wi 0.1 -> {wi_end}, Oldroyd-B beta=0.59, SQRT form, "
-                    f"{mesh.nel} Q2 quads ({len(rowptr) - 1} unknowns), LN0=1, dArN=0.01, "
-                    "Eps_Pr=1e-3, dS0=1, dS_max=50; host SuperLU (nested dissection) solve",
-        "arms": arms,
+    out.update({
         "speedup_wall": arms["plain_fp64"]["wall_s"] / arms["learned_fp32"]["wall_s"],
         "speedup_factorisations": arms["plain_fp64"]["factorisations"]
         / max(1, arms["learned_fp32"]["factorisations"]),
         "branch_max_rel_dev": dev,
+    })
+    return out
+
+
+def newton_precision_compare(nel: int, device: int = 0, wis=(0.1, 0.3, 0.5)):
+    """Precision form on one Newton solve per Weissenberg number: Giesekus
+    alpha = 0.1, beta = 0.59, SQRT form, natural continuation through ``wis``
+    from the fully developed start, each point to ||R|| < 1e-10 and
+    ||dx|| < 1e-10, once with the FP64 forward-difference Jacobian (the
+    reference algorithm; its iterates equal the oracle-driven Newton's bit for
+    bit) and once with the FP32 exact Jacobian beside the FP64 residual.
+    Reports iterations, factorisations and host time per solve, and the FP32
+    run's converged state against the FP64 one."""
+    from ve_flow_around_cylinder_fortran_gb300 import newton as NW
+    mesh = M.build_cylinder_mesh(nel)
+    phys = S.giesekus(0.1, wis[0], 0.59, "SQRT", nex=0)
+    rowptr, colind = P.build_pattern(mesh.element_nodes(), mesh.nnodes, phys.nex)
+    asm = V.BulkAssembler(mesh, phys, rowptr, colind, outlet_edges=True, device=device)
+    runs, final = {}, {}
+    for jac in ("fd64", "exact32"):
+        t0 = time.perf_counter()
+        res = NW.natural_continuation(asm, mesh, phys, list(wis), jacobian=jac, tol=1e-10)
+        wall = time.perf_counter() - t0
+        runs[jac] = {
+            "wall_s": wall,
+            "solves": [{"wi": wi, "iterations": r.iterations,
+                        "factorisations": sum(h["flag"] == "NRP" for h in r.history),
+                        "final_res_norm": r.history[-1]["res_norm"],
+                        "assembly_s": r.assembly_s, "factor_and_solve_s": r.solve_s}
+                       for wi, r in zip(wis, res)],
+        }
+        final[jac] = res[-1].TL
+    asm.close()
+    d = final["exact32"] - final["fd64"]
+    return {
+        "workload": f"Newton solves by natural continuation Wi = {', '.join(str(w) for w in wis)}, "
+                    f"Giesekus alpha=0.1, beta=0.59, SQRT form, {mesh.nel} Q2 quads "
+                    f"({len(rowptr) - 1} unknowns), outlet edges, Dirichlet rows on the device; "
+                    "host SuperLU (nested dissection)",
+        "fd64": runs["fd64"], "fp32_jacobian": runs["exact32"],
+        "solution_rel_err_2norm": float(np.linalg.norm(d) / np.linalg.norm(final["fd64"])),
+        "solution_rel_err_maxnorm": float(np.max(np.abs(d)) / np.max(np.abs(final["fd64"]))),
     }
 
 
@@ -543,10 +604,16 @@ def run_vefem(args):
                               "stability": stability_compare(args.nel, args.steps, args.warmup, dev,
                                                              cpu=False)}))
         return 0
+    if args.newton_only > 0:
+        if rank == 0:
+            print(json.dumps({"newton_precision": newton_precision_compare(args.newton_only, dev)}))
+        return 0
     if args.continuation_only:
         if rank == 0:
             out = continuation_compare(
                 args.cont_nel, args.cont_wi, dev, secant=not args.no_secant,
+                ablations=not args.no_ablations,
+                only=[a for a in args.cont_arms.split(",") if a] or None,
                 step_log=(lambda m: print(m, file=sys.stderr, flush=True)) if args.cont_log else None)
             print(json.dumps({"continuation": out}))
         if dist:
@@ -686,7 +753,8 @@ def run_vefem(args):
         line["batched"] = batched_compare(args.batch_inst, max(3, args.steps // 2), args.warmup, dev)
     if world == 1 and args.cont_nel > 0:
         line["continuation"] = continuation_compare(args.cont_nel, args.cont_wi, dev,
-                                                    secant=not args.no_secant)
+                                                    secant=not args.no_secant,
+                                                    ablations=not args.no_ablations)
     if world == 1 and args.stab_nel > 0:
         line["stability"] = stability_compare(args.stab_nel, max(3, args.steps // 4), args.warmup,
                                               dev, cpu=not args.no_cpu_baseline)

@@ -142,3 +142,36 @@ def test_unknown_reuse_policy_is_rejected():
     with pytest.raises(ValueError, match="reuse policy"):
         C.ArclengthContinuation(cont.asm, cont.mesh, cont.phys, "fd64",
                                 C.ArclengthSettings(reuse="sometimes"), assembly=cont.dev)
+
+
+def test_step_cutback_predicts_again_at_half_the_step():
+    """With cutbacks enabled a failed arclength solve halves dS and predicts
+    again from the last converged point (no relaxation); the step converges
+    on the arclength plane of the halved step."""
+    cont, TL, EU = _driver(max_steps=5)
+    cont.cfg = C.ArclengthSettings(dArN=0.01, max_steps=5, reuse="contraction", theta_max=0.6,
+                                   factor_cost=30.0, cutbacks=2)
+    orig = cont._newton
+    calls = {"n": 0, "x0": []}
+
+    def newton(x0, *a, **kw):
+        calls["n"] += 1
+        calls["x0"].append(x0.copy())
+        if calls["n"] == 4:                  # the first solve of increment 4
+            return x0, 1, 0, 1.0, None, False
+        return orig(x0, *a, **kw)
+
+    cont._newton = newton
+    recs, xs = cont.run(TL, EU)
+    r4 = recs[3]
+    assert r4.cutbacks == 1 and r4.emergencies == 0 and r4.res_norm < 1e-10
+    # the plain predictions x_o + t dS: the second lies half as far from the
+    # last converged point, along the same unit tangent
+    x3 = xs[2]
+    d1 = np.linalg.norm(calls["x0"][3] - x3)
+    d2 = np.linalg.norm(calls["x0"][4] - x3)
+    assert d2 == pytest.approx(0.5 * d1, rel=1e-12)
+    assert r4.dS == pytest.approx(d2, rel=1e-12)
+    # the converged point lies on the halved step's arclength plane
+    t = (calls["x0"][4] - x3) / d2
+    assert abs(np.dot(t, xs[3] - x3) - r4.dS) <= 1e-8 * r4.dS

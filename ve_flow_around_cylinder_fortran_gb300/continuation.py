@@ -76,6 +76,12 @@ class ArclengthSettings:
     factor_cost: float | None = None
     chord_max: int = 30       # at most this many predicted chord iterations
     theta_max: float = 1.0    # refactorise when a chord step contracts less than this
+    # step cutbacks before the reference's emergency (relaxation halving): a
+    # failed arclength solve halves dS and predicts again from the last
+    # converged point; a solve on a cutback-enabled step fails early once it
+    # has taken ``cutback_factorisations`` factorisations without converging
+    cutbacks: int = 0
+    cutback_factorisations: int = 6
 
 
 @dataclasses.dataclass
@@ -95,6 +101,7 @@ class StepRecord:
     solve_s: float = 0.0        # host triangular solves (Newton and tangent)
     predictor_s: float = 0.0    # learned predictor: prediction, judging, training
     emergencies: int = 0        # Newton restarts with relaxation (emergencyNewtonRaphson)
+    cutbacks: int = 0           # step cutbacks (dS halved, predicted again)
 
 
 class LambdaRow:
@@ -213,7 +220,8 @@ class ArclengthContinuation:
             return 10.0
         return self.t_fac / max(self.t_iter, 1e-9)
 
-    def _newton_chord(self, x0: np.ndarray, xF: float, max_iter: int, flag: str):
+    def _newton_chord(self, x0: np.ndarray, xF: float, max_iter: int, flag: str,
+                      max_fac: int | None = None):
         """Newton with the lambda row, reusing the last factorisation across
         solves (chord iterations) while it contracts well enough.  With a
         contraction rate theta = |s_k| / |s_(k-1)| observed on one
@@ -224,8 +232,9 @@ class ArclengthContinuation:
         contract (theta >= 1) is undone and the Jacobian assembled at the
         iterate it started from; after a Newton step on a factorisation taken
         at its own starting point the Jacobian is assembled at the new iterate
-        (the reference's 'MNR' -> 'NRP' switch).  Returns what _newton
-        returns."""
+        (the reference's 'MNR' -> 'NRP' switch).  With ``max_fac`` the solve
+        fails once it would take a factorisation beyond that many.  Returns
+        what _newton returns."""
         cfg = self.cfg
         x = x0.copy()
         tm = self.timers
@@ -243,6 +252,8 @@ class ArclengthContinuation:
             t0 = time.perf_counter()
             TL, EU = self.unpack(x)
             self._update_inflow(float(EU[0]))
+            if want and max_fac is not None and nfac >= max_fac:
+                return x, it, nfac, res_norm, lu, False
             b, vals = self.dev(TL, EU, want)
             self.lrow(x, b, vals)
             res_norm = float(np.linalg.norm(b))
@@ -310,13 +321,13 @@ class ArclengthContinuation:
             x = x - xF * s
 
     def _newton(self, x0: np.ndarray, xF: float = 1.0, max_iter: int = NW.NITER,
-                flag: str = "NRP"):
+                flag: str = "NRP", max_fac: int | None = None):
         """Newton with the lambda row and relaxation xF, starting in mode
         ``flag``; returns (x, iterations, factorisations, last residual norm,
         the solver holding the last factorisation, converged)."""
         cfg = self.cfg
         if cfg.reuse == "contraction":
-            return self._newton_chord(x0, xF, max_iter, flag)
+            return self._newton_chord(x0, xF, max_iter, flag, max_fac)
         x = x0.copy()
         tm = self.timers
         res_norm = cor_new = cor_old = 1.0
@@ -399,29 +410,33 @@ class ArclengthContinuation:
                 self.lrow.t, self.lrow.x_o, self.lrow.dS = t, x_o, dS
             pred_name = "plain"
             if predictor is not None and k > 2:
-                tp = time.perf_counter()
-                if hasattr(predictor, "candidates"):
-                    cands = predictor.candidates(k, x_o, t, dS, x_p)
-                    if cands:
-                        x_p, pred_name = self._judge([("plain", x_p)] + cands)
-                else:
-                    cand = predictor.predict(k, x_o, t, dS, x_p)
-                    if cand is not None and getattr(predictor, "replaces", False):
-                        x_p, pred_name = cand, type(predictor).__name__
-                    elif cand is not None:
-                        x_p, pred_name = self._judge([("plain", x_p), ("learned", cand)])
-                self.timers["predictor"] += time.perf_counter() - tp
+                x_p, pred_name = self._predict(predictor, k, x_o, t, dS, x_p)
+            # step cutbacks (cfg.cutbacks, the learned + mixed path): halve dS
+            # and predict again from the last converged point
             # emergencyNewtonRaphson (Newton_Raphson_mod.F90:533-584): restart
             # from the prediction with the relaxation halved, 50 x Niter
             # iterations allowed and, on the arclength branch, dSo halved
-            xF, max_it, its, nfac, emerg = 1.0, NW.NITER, 0, 0, 0
+            xF, max_it, its, nfac, emerg, cuts = 1.0, NW.NITER, 0, 0, 0, 0
             flag0 = self._start_flag(k)
             while True:
-                x, i1, f1, rn, lu, ok = self._newton(x_p, xF, max_it, flag0)
+                can_cut = k > 2 and cuts < cfg.cutbacks
+                x, i1, f1, rn, lu, ok = self._newton(
+                    x_p, xF, max_it, flag0, cfg.cutback_factorisations if can_cut else None)
                 its += i1
                 nfac += f1
                 if ok:
                     break
+                if can_cut:
+                    cuts += 1
+                    dS *= 0.5
+                    self.lrow.dS = dS
+                    x_p, pred_name = x_o + t * dS, "plain"
+                    if predictor is not None:
+                        x_p, pred_name = self._predict(predictor, k, x_o, t, dS, x_p)
+                    flag0 = "NRP"
+                    if self.log:
+                        self.log(f"step {k}: cutback to dS = {dS:.4g}")
+                    continue
                 xF *= 0.5
                 emerg += 1
                 if xF < 1.0e-2:
@@ -466,7 +481,7 @@ class ArclengthContinuation:
             tm = self.timers
             records.append(StepRecord(k, self.phys.Wi0 * lam, lam, dS, its, nfac, rn, pred_name,
                                       err_pr, wall, tm["assembly"], tm["factor"], tm["solve"],
-                                      tm["predictor"], emerg))
+                                      tm["predictor"], emerg, cuts))
             if self.log:
                 self.log(f"step {k}: Wi = {self.phys.Wi0 * lam:.4f}, Newton {its}, "
                          f"pred {pred_name} err {err_pr:.2e}, dS = {dS:.3f}, {wall:.2f} s")
@@ -481,6 +496,24 @@ class ArclengthContinuation:
             t = t_new
             x_p = x.copy() if t is None else x + t * dS
         return records, states
+
+    def _predict(self, predictor, k, x_o, t, dS, x_plain):
+        """The predictor's candidates for step length dS, judged against the
+        plain prediction x_plain; returns (x_p, name)."""
+        tp = time.perf_counter()
+        x_p, name = x_plain, "plain"
+        if hasattr(predictor, "candidates"):
+            cands = predictor.candidates(k, x_o, t, dS, x_plain)
+            if cands:
+                x_p, name = self._judge([("plain", x_plain)] + cands)
+        else:
+            cand = predictor.predict(k, x_o, t, dS, x_plain)
+            if cand is not None and getattr(predictor, "replaces", False):
+                x_p, name = cand, type(predictor).__name__
+            elif cand is not None:
+                x_p, name = self._judge([("plain", x_plain), ("learned", cand)])
+        self.timers["predictor"] += time.perf_counter() - tp
+        return x_p, name
 
     def _judge(self, cands):
         """Newton judges the predictions by residual norm: of the (name, x)
