@@ -82,10 +82,6 @@ class ArclengthSettings:
     # has taken ``cutback_factorisations`` factorisations without converging
     cutbacks: int = 0
     cutback_factorisations: int = 3
-    # direction of the arclength row and the plain prediction after increment
-    # 2: "tangent" (J t = e_lambda with the last factorisation, the reference)
-    # or "secant" ((x - x_o) / |x - x_o|, no solve)
-    direction: str = "tangent"
 
 
 @dataclasses.dataclass
@@ -185,8 +181,6 @@ class ArclengthContinuation:
         self.failed_factorisations = 0
         if self.cfg.reuse not in ("reference", "contraction"):
             raise ValueError(f"unknown factorisation reuse policy {self.cfg.reuse!r}")
-        if self.cfg.direction not in ("tangent", "secant"):
-            raise ValueError(f"unknown continuation direction {self.cfg.direction!r}")
         # running costs (s) of a chord iteration and of a factorisation, for
         # the "contraction" policy
         self.t_iter = None
@@ -471,7 +465,7 @@ class ArclengthContinuation:
             # direction (setDirectionVectors)
             if k == 1:
                 t_new = None
-            elif k == 2 or (cfg.direction == "secant" and not done):
+            elif k == 2:
                 d = x - x_o
                 t_new = d / np.linalg.norm(d)
             elif not done:
