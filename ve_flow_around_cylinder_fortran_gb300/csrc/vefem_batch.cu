@@ -153,7 +153,7 @@ void launch_all(vefem_batch *bt, int flags, bool timing, cudaError_t *err)
         }
     }
     if (timing && e == cudaSuccess) e = cudaEventRecord(bt->ev[1], s);
-    const int res_grid = bt->sms * std::max(1, residual_batched_ctas_per_sm(bt->form));
+    const int res_grid = bt->sms * std::max(1, residual_batched_ctas_per_sm(bt->form, bt->spec));
     const int ex_grid = bt->sms * std::max(1, exact_batched_ctas_per_sm((int)vsize, bt->form, bt->spec));
     const bool side = want_res && jmode;
     if (want_res && e == cudaSuccess) {
@@ -165,7 +165,7 @@ void launch_all(vefem_batch *bt, int flags, bool timing, cudaError_t *err)
         }
         if (e == cudaSuccess)
             e = launch_residual64_batched(bt->d_inst, bt->d_res_work, bt->n_res_work, bt->form,
-                                          std::min(res_grid, bt->n_res_work), rs);
+                                          bt->spec, std::min(res_grid, bt->n_res_work), rs);
         if (side && e == cudaSuccess) e = cudaEventRecord(bt->join, bt->s2);
         bt->launches++;
     }

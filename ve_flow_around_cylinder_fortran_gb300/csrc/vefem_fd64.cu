@@ -248,8 +248,9 @@ constexpr int RS_THREADS = RS_EPB * 9;
 // bound by the FP64 pipe, not by latency)
 constexpr int RS_MIN_CTAS = 3;
 
-// elements [e0, e0 + count) of one mesh, count <= RS_EPB
-template <int FORM>
+// elements [e0, e0 + count) of one mesh, count <= RS_EPB; SPEC leaves out the
+// exact-zero terms of ReN = 0 / DfN = 0 as the FD kernel does (same values)
+template <int FORM, int SPEC>
 __device__ __forceinline__ void res64_block(const ElemArgs &a, const KParams &prm, int e0,
                                             int count)
 {
@@ -286,11 +287,11 @@ __device__ __forceinline__ void res64_block(const ElemArgs &a, const KParams &pr
         SmemView V{s_tl[el]};
         auto I = interpolate(V, c_bfn[ig], dFx, dFy, d2x, d2y);
         double dotU[9];
-        auto g = gauss_point<FORM>(I, prm, WiN, go.H2, dFx, dFy, dotU);
+        auto g = gauss_point<FORM, SPEC>(I, prm, WiN, go.H2, dFx, dFy, dotU);
 #pragma unroll
         for (int n = 0; n < 9; n++)
-            test_node<FORM>(g, prm, c_bfn[ig][n], dFx[n], dFy[n], dotU[n], go.WET,
-                            &s_part[el][ig][n * 6]);
+            test_node<FORM, SPEC>(g, prm, c_bfn[ig][n], dFx[n], dFy[n], dotU[n], go.WET,
+                                  &s_part[el][ig][n * 6]);
     }
     __syncthreads();
     // in-order sum over the Gauss points (Res = Res + TERM*WET, ig = 1..9)
@@ -305,14 +306,14 @@ __device__ __forceinline__ void res64_block(const ElemArgs &a, const KParams &pr
     }
 }
 
-template <int FORM>
+template <int FORM, int SPEC>
 __global__ void __launch_bounds__(RS_THREADS, RS_MIN_CTAS) k_res64(const ElemArgs a, const KParams prm)
 {
-    res64_block<FORM>(a, prm, blockIdx.x * RS_EPB, RS_EPB);
+    res64_block<FORM, SPEC>(a, prm, blockIdx.x * RS_EPB, RS_EPB);
 }
 
 // persistent form over the work items of many meshes
-template <int FORM>
+template <int FORM, int SPEC>
 __global__ void __launch_bounds__(RS_THREADS, RS_MIN_CTAS)
 k_res64_batched(const BatchInst *__restrict__ insts, const WorkItem *__restrict__ work, int nwork)
 {
@@ -320,40 +321,62 @@ k_res64_batched(const BatchInst *__restrict__ insts, const WorkItem *__restrict_
         const WorkItem it = work[w];
         const ElemArgs a = insts[it.inst].ea;
         const KParams prm = insts[it.inst].prm;
-        res64_block<FORM>(a, prm, it.e0, it.count);
+        res64_block<FORM, SPEC>(a, prm, it.e0, it.count);
         __syncthreads();
     }
+}
+
+// the kernel's specialisation for the parameters: (form, which of ReN, DfN are zero)
+#define RES_DISPATCH(form, spec, LAUNCH)                                                        \
+    do {                                                                                        \
+        if ((form) == FORM_SQRT) {                                                              \
+            switch (spec) {                                                                     \
+            case 0: LAUNCH(FORM_SQRT, 0); break;                                                \
+            case SPEC_RE0: LAUNCH(FORM_SQRT, SPEC_RE0); break;                                  \
+            case SPEC_DF0: LAUNCH(FORM_SQRT, SPEC_DF0); break;                                  \
+            default: LAUNCH(FORM_SQRT, SPEC_RE0 | SPEC_DF0); break;                             \
+            }                                                                                   \
+        } else {                                                                                \
+            switch (spec) {                                                                     \
+            case 0: LAUNCH(FORM_T, 0); break;                                                   \
+            case SPEC_RE0: LAUNCH(FORM_T, SPEC_RE0); break;                                     \
+            case SPEC_DF0: LAUNCH(FORM_T, SPEC_DF0); break;                                     \
+            default: LAUNCH(FORM_T, SPEC_RE0 | SPEC_DF0); break;                                \
+            }                                                                                   \
+        }                                                                                       \
+    } while (0)
+
+static int spec_of(const KParams &p)
+{
+    return (p.ReN == 0.0 ? SPEC_RE0 : 0) | (p.DfN == 0.0 ? SPEC_DF0 : 0);
 }
 
 cudaError_t launch_residual64(const ElemArgs &a, const KParams &p, cudaStream_t s)
 {
     if (a.nel <= 0) return cudaSuccess;
     const int grid = (a.nel + RS_EPB - 1) / RS_EPB;
-    if (p.form == FORM_SQRT)
-        k_res64<FORM_SQRT><<<grid, RS_THREADS, 0, s>>>(a, p);
-    else
-        k_res64<FORM_T><<<grid, RS_THREADS, 0, s>>>(a, p);
+#define GO(F, SP) k_res64<F, SP><<<grid, RS_THREADS, 0, s>>>(a, p)
+    RES_DISPATCH(p.form, spec_of(p), GO);
+#undef GO
     return cudaGetLastError();
 }
 
 cudaError_t launch_residual64_batched(const BatchInst *insts, const WorkItem *work, int nwork,
-                                      int form, int grid, cudaStream_t s)
+                                      int form, int spec, int grid, cudaStream_t s)
 {
     if (nwork <= 0) return cudaSuccess;
-    if (form == FORM_SQRT)
-        k_res64_batched<FORM_SQRT><<<grid, RS_THREADS, 0, s>>>(insts, work, nwork);
-    else
-        k_res64_batched<FORM_T><<<grid, RS_THREADS, 0, s>>>(insts, work, nwork);
+#define GO(F, SP) k_res64_batched<F, SP><<<grid, RS_THREADS, 0, s>>>(insts, work, nwork)
+    RES_DISPATCH(form, spec, GO);
+#undef GO
     return cudaGetLastError();
 }
 
-int residual_batched_ctas_per_sm(int form)
+int residual_batched_ctas_per_sm(int form, int spec)
 {
     int n = 0;
-    if (form == FORM_SQRT)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_res64_batched<FORM_SQRT>, RS_THREADS, 0);
-    else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_res64_batched<FORM_T>, RS_THREADS, 0);
+#define GO(F, SP) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_res64_batched<F, SP>, RS_THREADS, 0)
+    RES_DISPATCH(form, spec, GO);
+#undef GO
     return n;
 }
 

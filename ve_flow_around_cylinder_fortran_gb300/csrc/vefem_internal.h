@@ -118,12 +118,12 @@ struct WorkItem {
     int inst, e0, count, pad;
 };
 cudaError_t launch_residual64_batched(const BatchInst *insts, const WorkItem *work, int nwork,
-                                      int form, int grid, cudaStream_t s);
+                                      int form, int spec, int grid, cudaStream_t s);
 template <class T>
 cudaError_t launch_exact_batched(const BatchInst *insts, const WorkItem *work, int nwork,
                                  int form, int spec, int grid, cudaStream_t s);
 // occupancy of the persistent kernels (resident CTAs per SM)
 int exact_batched_ctas_per_sm(int elem_size, int form, int spec);
-int residual_batched_ctas_per_sm(int form);
+int residual_batched_ctas_per_sm(int form, int spec);
 
 }  // namespace vefem

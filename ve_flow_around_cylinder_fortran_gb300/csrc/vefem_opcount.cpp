@@ -106,16 +106,12 @@ void count_element(const vefem::KParams &prm, const vefem::GaussTables &T, int w
                 if (pass == 1) interpolate_field(V, 3, T.bfn[ig], dFx[ig], dFy[ig], d2x[ig], d2y[ig], I);
             }
             Cd dotU[9];
-            auto g = want_jac ? gauss_point<FORM, SPEC>(I, prm, WiN, H2[ig], dFx[ig], dFy[ig], dotU)
-                              : gauss_point<FORM>(I, prm, WiN, H2[ig], dFx[ig], dFy[ig], dotU);
+            // both kernels leave out the exact-zero terms of ReN = 0 / DfN = 0
+            auto g = gauss_point<FORM, SPEC>(I, prm, WiN, H2[ig], dFx[ig], dFy[ig], dotU);
             for (int n = 0; n < 9; n++) {
                 Cd o[6];
-                if (want_jac)
-                    test_node<FORM, SPEC>(g, prm, T.bfn[ig][n], dFx[ig][n], dFy[ig][n], dotU[n],
-                                          WET[ig], o);
-                else
-                    test_node<FORM>(g, prm, T.bfn[ig][n], dFx[ig][n], dFy[ig][n], dotU[n],
-                                    WET[ig], o);
+                test_node<FORM, SPEC>(g, prm, T.bfn[ig][n], dFx[ig][n], dFy[ig][n], dotU[n],
+                                      WET[ig], o);
                 for (int f = 0; f < 6; f++) res[n * 6 + f] = res[n * 6 + f] + o[f];
             }
         }
