@@ -172,3 +172,29 @@ def test_trained_network_gains_over_extrapolation_alone():
             ss.append(s_star)
             pred.observe(k, truth, 0.1 + 0.05 * s_star)
         assert np.mean(err["learned"]) < 0.7 * np.mean(err["extrapolation"]), (h, err)
+
+
+def test_warm_up_leaves_the_predictor_unchanged():
+    """warm_up runs the predictor's code path on synthetic snapshots and
+    restores its state: the predictions after it equal those of a predictor
+    that was never warmed up, bit for bit."""
+    pytest.importorskip("torch")
+    from ve_flow_around_cylinder_fortran_gb300 import learned as LP
+    curve = _Curve()
+    out = []
+    for warm in (False, True):
+        ref = MLPRef(2 + 3 * 8, 8, width=16, hidden=1)
+        ref.init_params(0)
+        pred = LP.LearnedPredictor(n_modes=8, start=10, net=ref, device="cpu", iters=5)
+        if warm:
+            pred.warm_up(400)
+            assert pred.X == [] and pred.basis is None and pred.trainings == 0
+            assert pred.use_net and pred.timers == {"pod": 0.0, "train": 0.0, "predict": 0.0}
+        ss = list(np.linspace(0, 1.2, 12))
+        _feed(pred, curve, ss)
+        x1, x0 = curve(ss[-1]), curve(ss[-2])
+        t = (x1 - x0) / np.linalg.norm(x1 - x0)
+        out.append(pred.candidates(13, x1, t, 0.1, x1 + 0.1 * t))
+    assert [n for n, _ in out[0]] == [n for n, _ in out[1]] == ["learned", "extrapolation"]
+    for (_, a), (_, b) in zip(out[0], out[1]):
+        assert np.array_equal(a, b)

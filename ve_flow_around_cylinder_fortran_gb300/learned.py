@@ -87,24 +87,32 @@ class LearnedPredictor:
         self.order = order
 
     def warm_up(self, n: int, m: int = 6):
-        """Run the predictor's tensor operations (snapshot Gram matrix, mode
-        re-orthonormalisation, candidate reconstruction) once on synthetic
-        snapshots of length ``n``, so that the framework's first-use costs
-        (module loading and JIT of its kernels, several seconds on a fresh
-        process) fall outside a timed continuation.  The predictor's state
-        is unchanged."""
+        """Run the predictor's own code path (observe: snapshot upload, chord
+        length, Gram matrix and mode re-orthonormalisation; candidates:
+        features, extrapolation and reconstruction) on ``m`` or more synthetic
+        snapshots of length ``n``, without the network, so that the
+        framework's first-use costs (lazy loading and JIT of its kernels,
+        seconds on a fresh process) fall outside a timed continuation.  The
+        predictor's state is restored afterwards."""
         torch = self.torch
-        saved = (self.X, self.s, self.basis, self.coef)
+        keys = ("X", "wi", "s", "basis", "coef", "norm", "trained", "trainings", "last_loss",
+                "use_net")
+        saved = {k: getattr(self, k) for k in keys}
+        saved_timers = dict(self.timers)
         rng = np.random.default_rng(0)
+        x0, d1, d2 = (rng.standard_normal(n) for _ in range(3))
         try:
-            for mm in (m, m + 1):
-                self.X = [torch.from_numpy(rng.standard_normal(n)).to(self.dev) for _ in range(mm)]
-                mean, Phi, coef = self._pod()
-                self.basis = (mean, Phi)
-                a = coef[-1][:Phi.shape[1]]
-                (mean + Phi @ torch.from_numpy(np.ascontiguousarray(a)).to(self.dev)).cpu()
+            self.X, self.wi, self.s = [], [], [0.0]
+            self.basis = self.coef = self.norm = None
+            self.use_net = False
+            for j in range(max(m, self.predict_from + 1)):
+                self.observe(j + 1, x0 + j * d1 + 0.1 * j * j * d2, 0.1 * (j + 1))
+            x1 = x0 + j * d1
+            self.candidates(j + 2, x1, d1 / np.linalg.norm(d1), 1.0, x1 + d1)
         finally:
-            self.X, self.s, self.basis, self.coef = saved
+            for k, v in saved.items():
+                setattr(self, k, v)
+            self.timers = saved_timers
         if self.dev.type == "cuda":
             torch.cuda.synchronize(self.dev)
 
