@@ -36,7 +36,11 @@ iterations it predicts until the tolerance cost less than a factorisation;
 a stale factorisation that stops contracting is replaced at the iterate
 the failed chord step started from.  The residual, the tolerance and hence
 the converged points are the same; only the Jacobian the corrections are
-solved with is older.  The host solves
+solved with is older.  Step cutbacks (``ArclengthSettings.cutbacks``, also
+the learned + mixed path's) halve dS after a failed solve and predict again
+from the last converged point before the reference's relaxation restart, so
+the continuation follows the branch through folds instead of relaxing across
+them.  The host solves
 with SuperLU in a nested-dissection order (linsolve.py, stand-in for
 MUMPS); the dense lambda row and the arclength column make the matrix
 bordered, and the lambda unknown is ordered last.
