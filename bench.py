@@ -226,11 +226,13 @@ def algorithmic_ops(phys, flags):
     return out
 
 
-def cpu_oracle_rate(phys, mesh, TL, EU, rowptr, colind, target_s: float, reps: int):
-    """Elements/s of the oracle assembly on all host cores, on the first n
-    elements of the mesh, n sized for about target_s seconds per repetition."""
+def cpu_oracle_rate(phys, mesh, TL, EU, rowptr, colind, target_s: float, reps: int,
+                    threads: int = 0):
+    """Elements/s of the oracle assembly on ``threads`` host cores (0: all),
+    on the first n elements of the mesh, n sized for about target_s seconds
+    per repetition."""
     from oracle import oracle as O
-    cores = os.cpu_count() or 1
+    cores = threads or os.cpu_count() or 1
     conn = mesh.conn
     n0 = min(mesh.nel, 512)
     t = time.perf_counter()
@@ -762,10 +764,15 @@ def run_vefem(args):
     # cores afterwards and would slow the host side of the parts above
     if world == 1 and not args.no_cpu_baseline:
         rate, n, cores, times = cpu_oracle_rate(phys, mesh, TL, EU, rowptr, colind, 6.0, 3)
+        rate1, n1, _, times1 = cpu_oracle_rate(phys, mesh, TL, EU, rowptr, colind, 3.0, 3,
+                                               threads=1)
         line["cpu_baseline"] = {
             "value": rate, "unit": UNIT, "cores": cores, "kind": "port",
             "sample": f"first {n} of {nel} elements, residual + FD Jacobian into AIJ, "
-                      f"median of 3 ({', '.join(f'{x:.2f}' for x in times)} s)"}
+                      f"median of 3 ({', '.join(f'{x:.2f}' for x in times)} s)",
+            "one_core": {"value": rate1, "unit": UNIT,
+                         "sample": f"first {n1} of {nel} elements, median of 3 "
+                                   f"({', '.join(f'{x:.2f}' for x in times1)} s)"}}
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
