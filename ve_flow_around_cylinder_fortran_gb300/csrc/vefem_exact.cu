@@ -204,24 +204,54 @@ __device__ __forceinline__ void exact_element(const ElemArgs &a, const KParams &
     }
     __syncthreads();
 
-    // phase 2b: trial-function side, block layout ((i*9 + j)*36 + e*6 + f)
-    T *out = es + (size_t)e * 2916;
-    for (int o = t; o < 2916; o += EX_THREADS) {
-        const int ij = o / 36, r = o - 36 * (o / 36);
-        const int i = ij / 9, j = ij - 9 * (ij / 9);
-        const int q = r / 6, f = r - 6 * (r / 6);
-        const int ns = f < 2 ? 4 : 3;
-        T acc = 0;
+    // phase 2b: trial-function side.  Thread = (f, i, q), the 9 outputs of
+    // trial nodes j = 0..8: every A value is read once for all 9 (a thread
+    // per output read it 9 times; this phase was bound by shared-memory
+    // bandwidth), the trial-side factors are warp broadcasts, and each sum
+    // runs in the same order (Gauss point, then quantity).  f is the slowest
+    // index, so a warp's threads agree on the Laplacian term and read
+    // consecutive A entries.  The results go through shared memory (D is dead
+    // here) to the block layout ((i*9 + j)*36 + q*6 + f) with coalesced stores.
+    T *stage = D;
+    for (int w = t; w < 324; w += EX_THREADS) {
+        const int f = w / 54, iq = w - 54 * (w / 54);
+        const int i = iq / 6, q = iq - 6 * (iq / 6);
+        const int q0 = qdir(f, 0);
+        const bool lap = f < 2;
+        T acc[9];
+#pragma unroll
+        for (int j = 0; j < 9; j++) acc[j] = 0;
         for (int gp = 0; gp < 9; gp++) {
-            const T *ag = A + gp * EX_NDIR * EX_AST + i * 6 + q;
-            const int q0 = qdir(f, 0);
-            acc += ag[q0 * EX_AST] * s_bfn[gp][j];
-            acc += ag[(q0 + 1) * EX_AST] * s_dFx[gp][j];
-            acc += ag[(q0 + 2) * EX_AST] * s_dFy[gp][j];
-            if (ns == 4) acc += ag[(q0 + 3) * EX_AST] * s_lap[gp][j];
+            const T *ag = A + gp * EX_NDIR * EX_AST + iq;
+            const T a0 = ag[q0 * EX_AST], a1 = ag[(q0 + 1) * EX_AST], a2 = ag[(q0 + 2) * EX_AST];
+            if (lap) {
+                const T a3 = ag[(q0 + 3) * EX_AST];
+#pragma unroll
+                for (int j = 0; j < 9; j++) {
+                    T v = acc[j];
+                    v += a0 * s_bfn[gp][j];
+                    v += a1 * s_dFx[gp][j];
+                    v += a2 * s_dFy[gp][j];
+                    v += a3 * s_lap[gp][j];
+                    acc[j] = v;
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < 9; j++) {
+                    T v = acc[j];
+                    v += a0 * s_bfn[gp][j];
+                    v += a1 * s_dFx[gp][j];
+                    v += a2 * s_dFy[gp][j];
+                    acc[j] = v;
+                }
+            }
         }
-        out[o] = acc;
+#pragma unroll
+        for (int j = 0; j < 9; j++) stage[(i * 9 + j) * 36 + q * 6 + f] = acc[j];
     }
+    __syncthreads();
+    T *out = es + (size_t)e * 2916;
+    for (int o = t; o < 2916; o += EX_THREADS) out[o] = stage[o];
     if (prm.nex > 0 && t < 54) {
         T acc = 0;
         for (int gp = 0; gp < 9; gp++) acc += A[(gp * EX_NDIR + 20) * EX_AST + t];
