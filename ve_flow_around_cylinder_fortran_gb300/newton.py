@@ -295,7 +295,7 @@ class NewtonRaphson:
             t_asm += t1 - t0
             t_sol += t2 - t1
             cor_new = float(np.linalg.norm(s))
-            hist.append(dict(it=it, flag=flag if want_jac or flag == "MNR" else flag,
+            hist.append(dict(it=it, flag="NRP" if want_jac else "MNR",
                              res_norm=res_norm, cor_norm=cor_new))
             if log:
                 log(f"{it:4d}. {flag}: RES_NORM = {res_norm:.4e}, COR_NORM = {cor_new:.4e}")
