@@ -17,7 +17,8 @@
 // One element at a time per CTA of 192 threads (persistent: each CTA walks a
 // list of work items, each a run of consecutive elements of one mesh; a
 // single mesh is the one-instance case):
-//   phase 0  state and geometry (geometry in FP64, stored in T);
+//   phase 0  state and geometry, then the interpolated quantities per Gauss
+//            point;
 //   phase 1  thread (gp, d): D[gp][d][e*3+k] = dc_ek/dq_d;
 //   phase 2a A[gp][d][i*6+e] = WET sum_k psi_k(i) D[gp][d][e*3+k];
 //   phase 2b K(i,e; j,f) = sum_gp sum_s A[gp][q(f,s)][i*6+e] chi_s(j), and the
@@ -112,6 +113,7 @@ __device__ __forceinline__ void exact_element(const ElemArgs &a, const KParams &
     __shared__ T s_dFx[9][9], s_dFy[9][9], s_d2x[9][9], s_d2y[9][9], s_lap[9][9];
     __shared__ T s_H2[9], s_WET[9];
     __shared__ T s_bfn[9][9];          // basis values in T: no FP64 conversions in the loops
+    __shared__ Interp<T> s_ip[9];      // interpolated quantities per Gauss point
     const int t = threadIdx.x;
     if (t >= 96 && t < 96 + 81) s_bfn[(t - 96) / 9][(t - 96) % 9] = (T)x_bfn[(t - 96) / 9][(t - 96) % 9];
 
@@ -150,15 +152,20 @@ __device__ __forceinline__ void exact_element(const ElemArgs &a, const KParams &
         s_WET[ig] = go.WET;
     }
     __syncthreads();
+    // phase 0b: the 20 interpolated quantities of each Gauss point, once per
+    // element (the 21 direction threads of a Gauss point share them)
+    if (t < 9) {
+        TView<T> V{s_tl};
+        s_ip[t] = interpolate(V, s_bfn[t], s_dFx[t], s_dFy[t], s_d2x[t], s_d2y[t]);
+    }
+    __syncthreads();
 
     // phase 1: dc/dq along direction d at Gauss point gp
     if (t < 9 * EX_NDIR) {
         const int gp = t / EX_NDIR, d = t - EX_NDIR * (t / EX_NDIR);
         if (d < 20 || prm.nex > 0) {
             typedef Dual<T> R;
-            TView<T> V{s_tl};
-            const Interp<T> Ip = interpolate(V, s_bfn[gp], s_dFx[gp], s_dFy[gp], s_d2x[gp],
-                                             s_d2y[gp]);
+            const Interp<T> Ip = s_ip[gp];
             Interp<R> I;
 #define SEED(field, idx) I.field = R(Ip.field, d == (idx) ? (T)1 : (T)0)
             SEED(U1, 0); SEED(GU11, 1); SEED(GU21, 2); SEED(lap1, 3);
