@@ -175,3 +175,36 @@ def test_step_cutback_predicts_again_at_half_the_step():
     # the converged point lies on the halved step's arclength plane
     t = (calls["x0"][4] - x3) / d2
     assert abs(np.dot(t, xs[3] - x3) - r4.dS) <= 1e-8 * r4.dS
+
+
+class _GarbagePredictor:
+    """A predictor whose candidates are garbage: one not finite, one far off."""
+
+    def __init__(self):
+        self.calls = 0
+
+    def observe(self, k, x, wi):
+        pass
+
+    def candidates(self, k, x_o, t, dS, x_plain):
+        self.calls += 1
+        bad = x_plain.copy()
+        bad[::7] = np.nan
+        far = x_plain + 10.0
+        return [("learned", bad), ("extrapolation", far)]
+
+
+def test_garbage_predictions_are_rejected_by_the_residual_judge():
+    """Newton judges the candidates by residual norm: garbage from the
+    predictor (NaN entries, a far-off state) is never taken, and the run
+    equals the one without a predictor bit for bit."""
+    ref, TL, EU = _driver(max_steps=6)
+    r0, x0 = ref.run(TL, EU)
+    cont, TL, EU = _driver(max_steps=6)
+    pred = _GarbagePredictor()
+    r1, x1 = cont.run(TL, EU, predictor=pred)
+    assert pred.calls == 4                              # increments 3..6
+    assert all(r.predictor == "plain" for r in r1)
+    assert len(r0) == len(r1)
+    for a, b in zip(x0, x1):
+        assert np.array_equal(a, b)
