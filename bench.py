@@ -285,7 +285,7 @@ def run_reference(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "config": cfg,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": sample},
+                         "sample": sample, "flags": O.build_flags(), "cpu_model": O.cpu_model()},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference (Fortran + PETSc + MPI) cannot be built on this machine or the "
                 "GPU box (no Fortran compiler); its algorithm runs as the C oracle port, "
@@ -766,8 +766,10 @@ def run_vefem(args):
         rate, n, cores, times = cpu_oracle_rate(phys, mesh, TL, EU, rowptr, colind, 6.0, 3)
         rate1, n1, _, times1 = cpu_oracle_rate(phys, mesh, TL, EU, rowptr, colind, 3.0, 3,
                                                threads=1)
+        from oracle import oracle as O
         line["cpu_baseline"] = {
             "value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+            "flags": O.build_flags(), "cpu_model": O.cpu_model(),
             "sample": f"first {n} of {nel} elements, residual + FD Jacobian into AIJ, "
                       f"median of 3 ({', '.join(f'{x:.2f}' for x in times)} s)",
             "one_core": {"value": rate1, "unit": UNIT,

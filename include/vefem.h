@@ -185,12 +185,17 @@ int vefem_algorithmic_ops(const vefem_params *params, int flags, double *out);
  * 1-based), xyz [3*nnodes], TL [6*nnodes], EU [nex], b [nnodes*6 + nex];
  * the residual is ADDED into b (rows of the arclength unknown untouched),
  * bit-identical to vefem_assemble(VEFEM_RESIDUAL).  stream: a cudaStream_t
- * (NULL = default stream); the call returns after the stream has finished.
+ * (NULL = default stream); the call synchronises that stream (it reads a
+ * device-side error flag) before it returns, and it leaves the caller's
+ * current device as it found it.
  * Scratch is one static device array of about 17.7 MB that every GPU loading
- * the library holds until exit; meshes above 32768 elements or 294912 nodes
- * are rejected with VEFEM_ERR_ARG.  The first call on a device looks up that
- * array's address and uploads the Gauss tables: make it before any stream
- * capture.  All calls share the array: calls that overlap on the GPU race. */
+ * the library holds until exit.  Limits, each rejected with VEFEM_ERR_ARG:
+ * at most 32768 elements and 294912 nodes (checked before anything runs);
+ * at most 32 elements sharing one node, and connectivity ids in 1..nnodes
+ * (checked on the device before anything is added: b is left unchanged).
+ * The first call on a device looks up that array's address and uploads the
+ * Gauss tables: make it before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU race. */
 int vefem_assemble_residual_noalloc(const vefem_params *params, int nnodes, int nel,
                                     const int32_t *conn, const double *xyz, const double *TL,
                                     const double *EU, double *b, void *stream);

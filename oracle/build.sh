@@ -2,11 +2,16 @@
 # Builds the CPU oracle (test infrastructure) into oracle/_build/.
 # vefem_stability_oracle.c includes vefem_oracle.c: one library with both.
 # -ffp-contract=off: no FMA contraction, plain IEEE binary64 in source order.
+# -O3 for the timed CPU baseline; no -march=native: the same source is built on
+# x86-64 here and on the aarch64 GPU host, and must give the same bits on both
+# (with contraction off, vector code would not change any result anyway).
+# The flags are written next to the library so the benchmark can report them.
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 mkdir -p "$HERE/_build"
 OMP="-fopenmp"
 if ! echo 'int main(void){return 0;}' | gcc -x c -fopenmp - -o /dev/null 2>/dev/null; then OMP=""; fi
-gcc -O2 -std=c11 -ffp-contract=off -fno-fast-math -fPIC -shared $OMP \
-    -o "$HERE/_build/libvefem_oracle.so.tmp" "$HERE/vefem_stability_oracle.c" -lm
+FLAGS="-O3 -std=c11 -ffp-contract=off -fno-fast-math -fPIC -shared $OMP"
+gcc $FLAGS -o "$HERE/_build/libvefem_oracle.so.tmp" "$HERE/vefem_stability_oracle.c" -lm
 mv "$HERE/_build/libvefem_oracle.so.tmp" "$HERE/_build/libvefem_oracle.so"
+echo "gcc $(gcc -dumpfullversion) $FLAGS" > "$HERE/_build/flags.txt"

@@ -27,6 +27,32 @@ def build(force: bool = False) -> str:
     return SO
 
 
+def build_flags() -> str:
+    """Compiler and flags the oracle library was built with."""
+    path = os.path.join(HERE, "_build", "flags.txt")
+    return open(path).read().strip() if os.path.exists(path) else "unknown"
+
+
+def cpu_model() -> str:
+    """Host CPU model name (x86 'model name', or the Arm implementer/part)."""
+    try:
+        txt = open("/proc/cpuinfo").read()
+    except OSError:
+        return "unknown"
+    for line in txt.splitlines():
+        if line.lower().startswith("model name"):
+            return line.split(":", 1)[1].strip()
+    parts = {}
+    for line in txt.splitlines():
+        if ":" in line:
+            k, v = line.split(":", 1)
+            parts.setdefault(k.strip(), v.strip())
+    arm_parts = {"0xd4f": "Neoverse-V2", "0xd40": "Neoverse-V1", "0xd0c": "Neoverse-N1"}
+    if "CPU part" in parts:
+        return "Arm " + arm_parts.get(parts["CPU part"], "part " + parts["CPU part"])
+    return "unknown"
+
+
 def lib():
     global _lib
     if _lib is None:

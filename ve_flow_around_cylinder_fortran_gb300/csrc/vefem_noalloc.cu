@@ -3,26 +3,32 @@
 // Who needs it: callers that cannot call cudaMalloc when they assemble -- a
 // host whose device memory is owned by another allocator (a PETSc/Kokkos
 // memory pool, a framework that reserves the whole GPU at start-up), code
-// that runs inside a section where allocation is forbidden (real-time loops,
-// regions that must not synchronise the device), or hosts that cannot keep a
-// library context alive between calls.  vefem_assemble needs a context whose
-// tables and scratch are allocated on the device; this entry point needs
-// none: the caller passes device inputs and the device output, and the
-// scratch (element residuals, node incidence lists) lives in one file-scope
-// static device array of fixed size that every GPU loading the library holds
-// until the process exits.
+// that runs inside a section where allocation is forbidden (real-time
+// loops), or hosts that cannot keep a library context alive between calls.
+// vefem_assemble needs a context whose tables and scratch are allocated on
+// the device; this entry point needs none: the caller passes device inputs
+// and the device output, and the scratch (element residuals, node incidence
+// lists) lives in one file-scope static device array of fixed size that
+// every GPU loading the library holds until the process exits.
 //
 // Limits and rules:
 //  * at most NOALLOC_MAX_EL elements and NOALLOC_MAX_NODES nodes per call
 //    (about 17.7 MB of static scratch); larger meshes are rejected with
 //    VEFEM_ERR_ARG before anything runs;
+//  * at most NOALLOC_MAX_NODE_ELEMS elements may share one node, and every
+//    connectivity id must lie in 1..nnodes; both are checked on the device
+//    before anything is added into b, and a violation returns VEFEM_ERR_ARG
+//    with b unchanged;
 //  * the first call on a device, with that device current, looks up the
 //    scratch array's device address (cudaGetSymbolAddress) and uploads the
 //    Gauss tables; make that first call before any stream capture;
+//  * every call waits for its stream to finish before it returns (it reads
+//    the device-side error flag), and it leaves the caller's current device
+//    as it found it;
 //  * every call shares the one scratch array and leaves its contents behind;
-//    the parts that must start at zero (the node counters) are cleared by the
-//    call itself.  Calls that overlap on the GPU (other streams, other host
-//    threads) race on the scratch: serialise them.
+//    the parts that must start at zero (the node counters, the error flag)
+//    are cleared by the call itself.  Calls that overlap on the GPU (other
+//    streams, other host threads) race on the scratch: serialise them.
 //
 // The result is the same, bit for bit, as vefem_assemble(VEFEM_RESIDUAL):
 // element residuals from the same physics source, then per row an in-order
@@ -156,7 +162,14 @@ __global__ void __launch_bounds__(1024) k_na_scan(int nnodes, NoAllocScratch *S)
     const int i0 = t * per;
     const int i1 = min(i0 + per, nnodes);
     int32_t local = 0;
-    for (int i = i0; i < i1; i++) local += S->cnt[i];
+    bool crowded = false;
+    for (int i = i0; i < i1; i++) {
+        local += S->cnt[i];
+        crowded |= S->cnt[i] > NOALLOC_MAX_NODE_ELEMS;
+    }
+    // a node with too many elements fails the call before k_na_gather adds
+    // anything into b (same value from every writer)
+    if (crowded && S->err == 0) S->err = 1;
     s_sum[t] = local;
     __syncthreads();
     for (int d = 1; d < 1024; d <<= 1) {
@@ -189,13 +202,9 @@ __global__ void k_na_fill(int nel, const int32_t *conn, NoAllocScratch *S)
 __global__ void k_na_gather(int nnodes, double *b, NoAllocScratch *S)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nnodes * 6 || S->err == 2) return;
+    if (t >= nnodes * 6 || S->err) return;   // b stays untouched on every error
     const int node = t / 6, jeq = t - 6 * (t / 6);
     const int c0 = S->off[node], n = S->off[node + 1] - c0;
-    if (n > NOALLOC_MAX_NODE_ELEMS) {
-        S->err = 1;
-        return;
-    }
     int32_t c[NOALLOC_MAX_NODE_ELEMS];
     for (int k = 0; k < n; k++) {
         const int32_t v = S->list[c0 + k];
@@ -272,7 +281,15 @@ extern "C" int vefem_assemble_residual_noalloc(const vefem_params *params, int n
         return na_fail(VEFEM_ERR_ARG, std::string(me) + "nnodes = " + std::to_string(nnodes) +
                                           " exceeds the static scratch limit of " +
                                           std::to_string(NOALLOC_MAX_NODES) + " nodes");
-    cudaError_t e = cudaSetDevice(params->device);
+    int prev_device = -1;
+    cudaError_t e = cudaGetDevice(&prev_device);
+    if (e != cudaSuccess) return na_fail(VEFEM_ERR_CUDA, std::string(me) + cudaGetErrorString(e));
+    // the caller's current device is restored on every return below
+    struct DeviceGuard {
+        int dev;
+        ~DeviceGuard() { cudaSetDevice(dev); }
+    } guard{prev_device};
+    e = cudaSetDevice(params->device);
     NoAllocScratch *S = nullptr;
     if (e == cudaSuccess) e = setup_device(params->device, &S);
     if (e != cudaSuccess) return na_fail(VEFEM_ERR_CUDA, std::string(me) + cudaGetErrorString(e));
