@@ -14,15 +14,17 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SO = os.path.join(HERE, "_build", "libvefem_oracle.so")
+SO_CS = os.path.join(HERE, "_build", "libvefem_oracle_cs.so")
 
 _lib = None
+_cs = None
 
 
 def build(force: bool = False) -> str:
     srcs = [os.path.join(HERE, f) for f in ("vefem_oracle.c", "vefem_stability_oracle.c",
                                            "build.sh")]
-    if force or not os.path.exists(SO) or any(os.path.getmtime(SO) < os.path.getmtime(f)
-                                              for f in srcs):
+    if force or not os.path.exists(SO) or not os.path.exists(SO_CS) or any(
+            os.path.getmtime(x) < os.path.getmtime(f) for f in srcs for x in (SO, SO_CS)):
         subprocess.check_call(["bash", os.path.join(HERE, "build.sh")])
     return SO
 
@@ -72,6 +74,20 @@ def lib():
             f.restype = I
         _lib = L
     return _lib
+
+
+def cs_lib():
+    """The oracle built on complex numbers (complex-step exact Jacobian)."""
+    global _cs
+    if _cs is None:
+        build()
+        L = ctypes.CDLL(SO_CS)
+        P = ctypes.c_void_p
+        I = ctypes.c_int
+        L.ora_cs_element_batch.argtypes = [P, P, I, I, P, P, P, P, I, I, P, P, P, I]
+        L.ora_cs_element_batch.restype = I
+        _cs = L
+    return _cs
 
 
 def _p(a):
@@ -175,3 +191,53 @@ def stability_elements(phys, conn, xyz, TLb, TLd, KwN: float, kz: bool = True, j
     if rc:
         raise ValueError(f"ora_stability_batch: {rc} (T form and non-FENE models only)")
     return ra, rb, A, B
+
+
+def exact_element_outputs(phys, conn, xyz, TL, EU, e0=0, e1=None, nthreads=0):
+    """Element residuals [n, 9, 6], exact Jacobians [n, 9, 6, 9, 6] by the
+    complex step (layout of element_outputs) and exact Ac columns [n, 9, 6, nex]."""
+    ip, dp, conn, xyz, TL, EU = _prep(phys, conn, xyz, TL, EU)
+    nel = conn.shape[1]
+    nn = xyz.shape[1]
+    e1 = nel if e1 is None else e1
+    n = e1 - e0
+    res = np.zeros((n, 9, 6))
+    jac = np.zeros((n, 9, 6, 9, 6))
+    ac = np.zeros((n, 9, 6, max(phys.nex, 1)))
+    rc = cs_lib().ora_cs_element_batch(_p(ip), _p(dp), nel, nn, _p(conn), _p(xyz), _p(TL),
+                                       _p(EU), e0, e1, _p(res), _p(jac), _p(ac), nthreads)
+    assert rc == 0
+    return res, jac, ac[..., :phys.nex]
+
+
+def exact_assemble(phys, conn, xyz, TL, EU, rowptr, colind, nthreads=0):
+    """Exact (complex-step) Jacobian of the bulk assembly into CSR values:
+    row (jnod, jeq) equation, column (inod, ieq) unknown, and the arclength
+    column (the last entry of every node row), added in element order
+    (storeResidual / storeJacobian / storeJacobian_Ac, Storage_mod.F90:10-115).
+    Returns (b, vals)."""
+    conn = np.ascontiguousarray(conn, dtype=np.int32)
+    nel = conn.shape[1]
+    en = conn.T.astype(np.int64) - 1
+    N = len(rowptr) - 1
+    rowptr = np.asarray(rowptr, dtype=np.int64)
+    colind = np.asarray(colind, dtype=np.int64)
+    keys = np.repeat(np.arange(N, dtype=np.int64), np.diff(rowptr)) * N + colind
+    b = np.zeros(N)
+    vals = np.zeros(len(colind))
+    chunk = 2048
+    for e0 in range(0, nel, chunk):
+        e1 = min(nel, e0 + chunk)
+        res, jac, ac = exact_element_outputs(phys, conn, xyz, TL, EU, e0, e1, nthreads)
+        dof = (en[e0:e1, :, None] * 6 + np.arange(6)[None, None, :]).reshape(e1 - e0, 54)
+        np.add.at(b, dof.reshape(-1), res.reshape(-1))
+        # A[row = (jnod, jeq), col = (inod, ieq)] = jac[inod, ieq, jnod, jeq]
+        blk = jac.reshape(e1 - e0, 54, 54).transpose(0, 2, 1)
+        q = (dof[:, :, None] * N + dof[:, None, :]).reshape(-1)
+        slots = np.searchsorted(keys, q)
+        if np.any(slots >= len(keys)) or np.any(keys[np.minimum(slots, len(keys) - 1)] != q):
+            raise RuntimeError("exact assembly: element entry missing from the pattern")
+        np.add.at(vals, slots, blk.reshape(-1))
+        if phys.nex:
+            np.add.at(vals, rowptr[dof.reshape(-1) + 1] - 1, ac[..., 0].reshape(-1))
+    return b, vals

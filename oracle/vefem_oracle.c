@@ -33,6 +33,28 @@
 #include <omp.h>
 #endif
 
+/* Scalar type of the state-dependent arithmetic.  The default build is plain
+ * binary64.  Built with -DORA_COMPLEX_STEP the same routines run on complex
+ * numbers, and ora_cs_element_batch (end of file) differentiates residualBulk
+ * by the complex step: column j of the element Jacobian is
+ * Im(Res(x + i h e_j)) / h with h = 1e-30 (Squire & Trapp, SIAM Rev. 40, 1998;
+ * Martins, Sturdza & Alonso, ACM TOMS 29, 2003).  No difference is taken, so
+ * the column is exact to rounding: an oracle for the exact (linearised)
+ * Jacobian, independent of the library's forward-mode dual numbers.  |x| is
+ * continued as sign(Re x) x, the derivative of the absolute value away from 0. */
+#ifdef ORA_COMPLEX_STEP
+#include <complex.h>
+typedef double _Complex real_t;
+static inline real_t RABS(real_t z) { return creal(z) < 0.0 ? -z : z; }
+#define RSQRT(z) csqrt(z)
+#define REXP(z) cexp(z)
+#else
+typedef double real_t;
+#define RABS(z) fabs(z)
+#define RSQRT(z) sqrt(z)
+#define REXP(z) exp(z)
+#endif
+
 #define NBF 9
 #define NEQ 6
 #define NGP 9
@@ -61,25 +83,25 @@ typedef struct {
 
 /* GaussPointQuantities, Global_Variables_mod.F90:56-84 (fields on this path) */
 typedef struct {
-    double GU[3][3], GUT[3][3], G_dot[3][3], GU_tr[3][3], GUT_tr[3][3], G_dot_tr[3][3];
-    double P_tot[3][3], G2U[3][3];
-    double U_f[3], dPdXi[3], dUfdt[3];
-    double Momentum[3], Convection[3];
-    double Continuity, P;
-    double dTdXi[3][3][3], dCdXi[3][3][3], dSdXi[3][3][3];
-    double S[3][3], dSdt[3][3];
-    double Con_EQ[3][3], T_ve[3][3], C_Tensor[3][3];
-    double f[3], g[2], dgdxi[2][3], f_T;
+    real_t GU[3][3], GUT[3][3], G_dot[3][3], GU_tr[3][3], GUT_tr[3][3], G_dot_tr[3][3];
+    real_t P_tot[3][3], G2U[3][3];
+    real_t U_f[3], dPdXi[3], dUfdt[3];
+    real_t Momentum[3], Convection[3];
+    real_t Continuity, P;
+    real_t dTdXi[3][3][3], dCdXi[3][3][3], dSdXi[3][3][3];
+    real_t S[3][3], dSdt[3][3];
+    real_t Con_EQ[3][3], T_ve[3][3], C_Tensor[3][3];
+    real_t f[3], g[2], dgdxi[2][3], f_T;
     double dXidci[3][3];
     double detJ, WET;
-    double mag_con_EQ, tlsic, tlsme, tlsce, tdcs;
+    real_t mag_con_EQ, tlsic, tlsme, tlsce, tdcs;
 } gp_t;
 
 /* NodeArrays, Global_Variables_mod.F90:86-110 (fields on this path) */
 typedef struct {
-    double tl[NBF][NEQ];
-    double eu[2];
-    double xi[NBF][3];
+    real_t tl[NBF][NEQ];
+    real_t eu[2];
+    double xi[NBF][3];                       /* geometry is never perturbed */
     double dFdXi[3][NBF], d2FdXi2[3][NBF];
     const double *bfn, *dfdc, *dfde, *d2fdc2, *d2fde2, *d2fdce;
 } elem_t;
@@ -204,44 +226,44 @@ static void gauss_edge_tables(int ied, double w[3], double bfn[3][NBF], double d
 /* Tools_mod.F90                                                           */
 
 /* traceTensorReal :206-220 */
-static double trace3(const double A[3][3])
+static real_t trace3(const real_t A[3][3])
 {
-    double t = 0.0;
+    real_t t = 0.0;
     for (int i = 0; i < 3; i++) t = t + A[i][i];
     return t;
 }
 
 /* doubleDotProductReal :262-278 -- A:B^T, i outer, j inner */
-static double ddot3(const double A[3][3], const double B[3][3])
+static real_t ddot3(const real_t A[3][3], const real_t B[3][3])
 {
-    double s = 0.0;
+    real_t s = 0.0;
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++) s = s + A[i][j] * B[j][i];
     return s;
 }
 
 /* Fortran matmul for 3x3: C(i,j) = sum_k A(i,k) B(k,j), k ascending from zero */
-static void matmul3(const double A[3][3], const double B[3][3], double C[3][3])
+static void matmul3(const real_t A[3][3], const real_t B[3][3], real_t C[3][3])
 {
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++) {
-            double s = 0.0;
+            real_t s = 0.0;
             for (int k = 0; k < 3; k++) s = s + A[i][k] * B[k][j];
             C[i][j] = s;
         }
 }
 
 /* dot_product over the 9 element nodes */
-static double dot9(const double *a, int sa, const double *b)
+static real_t dot9(const real_t *a, int sa, const double *b)
 {
-    double s = 0.0;
+    real_t s = 0.0;
     for (int n = 0; n < NBF; n++) s = s + a[n * sa] * b[n];
     return s;
 }
 
-static double dot3(const double *a, const double *b)
+static real_t dot3(const real_t *a, const real_t *b)
 {
-    double s = 0.0;
+    real_t s = 0.0;
     for (int n = 0; n < 3; n++) s = s + a[n] * b[n];
     return s;
 }
@@ -255,9 +277,9 @@ static void stress_component(int i, int istart, int *j, int *k)
 }
 
 /* inverseTensor2D :129-146 with determinant2D :78-87 */
-static void inverse2(const double A[2][2], double AI[2][2])
+static void inverse2(const real_t A[2][2], real_t AI[2][2])
 {
-    double detA = A[0][0] * A[1][1] - A[0][1] * A[1][0];
+    real_t detA = A[0][0] * A[1][1] - A[0][1] * A[1][0];
     AI[0][0] = A[1][1];
     AI[0][1] = -A[0][1];
     AI[1][0] = -A[1][0];
@@ -364,9 +386,9 @@ static void set_flow_kinematics(gp_t *g)
         for (int j = 0; j < 3; j++) g->G_dot[i][j] = g->GU[i][j] + g->GUT[i][j];
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++) g->GU_tr[i][j] = g->GU[i][j];
-    double tr = trace3(g->GU);
+    real_t tr = trace3(g->GU);
     for (int i = 0; i < N; i++)
-        for (int j = 0; j < N; j++) g->GU_tr[i][j] = g->GU[i][j] - tr * I3[i][j] / (double)N;
+        for (int j = 0; j < N; j++) g->GU_tr[i][j] = g->GU[i][j] - tr * I3[i][j] / (real_t)N;
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++) g->GUT_tr[i][j] = g->GU_tr[j][i];
     for (int i = 0; i < 3; i++)
@@ -377,26 +399,26 @@ static void set_flow_kinematics(gp_t *g)
 /* Constitutive_Models_mod.F90 (T form)                                    */
 
 /* setFENEMaterialDerivative :272-311, steady (no Transient term) */
-static double fene_material_derivative(const prm_t *p, double WiN, const gp_t *g)
+static real_t fene_material_derivative(const prm_t *p, real_t WiN, const gp_t *g)
 {
-    double dfdXi[3] = {0.0, 0.0, 0.0};
+    real_t dfdXi[3] = {0.0, 0.0, 0.0};
     for (int i = 0; i < 3; i++)
         for (int c = 0; c < 3; c++) dfdXi[c] = dfdXi[c] + g->dTdXi[i][i][c];
     if (p->model == M_FENE_P) {
         for (int c = 0; c < 3; c++) dfdXi[c] = (WiN / (1.0 - p->BvN)) * dfdXi[c] / p->VeN;
     } else {
         for (int c = 0; c < 3; c++)
-            dfdXi[c] = (WiN / (1.0 - p->BvN)) * dfdXi[c] / (p->VeN - (double)NDIM);
+            dfdXi[c] = (WiN / (1.0 - p->BvN)) * dfdXi[c] / (p->VeN - (real_t)NDIM);
     }
-    double MDfDt = 0.0;
+    real_t MDfDt = 0.0;
     for (int i = 0; i < 3; i++) MDfDt = MDfDt + g->U_f[i] * dfdXi[i];
     return MDfDt;
 }
 
 /* conEQ_* :96-268 */
-static void con_eq_T(const prm_t *p, double WiN, gp_t *g)
+static void con_eq_T(const prm_t *p, real_t WiN, gp_t *g)
 {
-    double trT = trace3(g->S);
+    real_t trT = trace3(g->S);
     double BvN = p->BvN, VeN = p->VeN;
     switch (p->model) {
     case M_L_PTT:
@@ -410,12 +432,12 @@ static void con_eq_T(const prm_t *p, double WiN, gp_t *g)
         g->g[0] = g->f_T; g->g[1] = g->g[0];
         break;
     case M_E_PTT:
-        g->f_T = exp(VeN * WiN * trT / (1.0 - BvN));
+        g->f_T = REXP(VeN * WiN * trT / (1.0 - BvN));
         g->f[0] = 1.0; g->f[1] = g->f_T; g->f[2] = 0.0;
         g->g[0] = 1.0; g->g[1] = 1.0;
         break;
     case M_M_E_PTT:
-        g->f_T = exp(VeN * WiN * trT / (1.0 - BvN));
+        g->f_T = REXP(VeN * WiN * trT / (1.0 - BvN));
         g->f[0] = g->f_T; g->f[1] = g->f[0]; g->f[2] = 0.0;
         g->g[0] = g->f_T; g->g[1] = g->g[0];
         break;
@@ -425,9 +447,9 @@ static void con_eq_T(const prm_t *p, double WiN, gp_t *g)
         g->g[0] = 1.0; g->g[1] = 1.0;
         break;
     case M_FENE_CR: {
-        g->f_T = 1.0 + ((WiN * trT / (1.0 - BvN))) / (VeN - (double)NDIM);
+        g->f_T = 1.0 + ((WiN * trT / (1.0 - BvN))) / (VeN - (real_t)NDIM);
         g->f[0] = g->f_T;
-        double MDfDt = fene_material_derivative(p, WiN, g);
+        real_t MDfDt = fene_material_derivative(p, WiN, g);
         g->f[1] = g->f_T - (WiN * MDfDt / g->f_T);
         g->f[2] = 0.0;
         g->g[0] = g->f_T; g->g[1] = g->g[0];
@@ -436,7 +458,7 @@ static void con_eq_T(const prm_t *p, double WiN, gp_t *g)
     default: { /* M_FENE_P */
         g->f_T = 1.0 + (WiN * trT / (1.0 - BvN)) / VeN;
         g->f[0] = 1.0;
-        double MDfDt = fene_material_derivative(p, WiN, g);
+        real_t MDfDt = fene_material_derivative(p, WiN, g);
         g->f[1] = g->f_T - (WiN * MDfDt / g->f_T);
         g->f[2] = 0.0;
         g->g[0] = 1.0; g->g[1] = g->f_T;
@@ -446,7 +468,7 @@ static void con_eq_T(const prm_t *p, double WiN, gp_t *g)
 }
 
 /* setStressTensor :335-349 */
-static void set_stress_tensor_T(const prm_t *p, double WiN, gp_t *g)
+static void set_stress_tensor_T(const prm_t *p, real_t WiN, gp_t *g)
 {
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++)
@@ -459,7 +481,7 @@ static void set_stress_tensor_T(const prm_t *p, double WiN, gp_t *g)
 }
 
 /* strongFormConEQ :55-92 with setUpperConvectedDerivativeT :315-331 */
-static void strong_form_con_eq_T(const prm_t *p, double WiN, gp_t *g)
+static void strong_form_con_eq_T(const prm_t *p, real_t WiN, gp_t *g)
 {
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++) {
@@ -469,7 +491,7 @@ static void strong_form_con_eq_T(const prm_t *p, double WiN, gp_t *g)
     con_eq_T(p, WiN, g);
     set_stress_tensor_T(p, WiN, g);
 
-    double UCD[3][3], M1[3][3], M2[3][3], Tve2[3][3];
+    real_t UCD[3][3], M1[3][3], M2[3][3], Tve2[3][3];
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++) UCD[i][j] = g->dSdt[i][j];
     for (int k = 0; k < 3; k++)
@@ -481,14 +503,14 @@ static void strong_form_con_eq_T(const prm_t *p, double WiN, gp_t *g)
         for (int j = 0; j < 3; j++) UCD[i][j] = UCD[i][j] - M1[i][j] - M2[i][j];
     matmul3(g->S, g->S, Tve2);
 
-    double term_I = 0.0;
+    real_t term_I = 0.0;
     if (p->model == M_FENE_P) {
-        double MDfDt = fene_material_derivative(p, WiN, g);
+        real_t MDfDt = fene_material_derivative(p, WiN, g);
         term_I = MDfDt / (g->f_T);
     }
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++) {
-            double c = WiN * UCD[i][j] + (g->f[2]) * Tve2[i][j];
+            real_t c = WiN * UCD[i][j] + (g->f[2]) * Tve2[i][j];
             c = c + (g->f[1]) * g->S[i][j];
             c = c - g->f[0] * (1.0 - p->BvN) * (g->G_dot_tr[i][j] + term_I * I3[i][j]);
             g->Con_EQ[i][j] = c;
@@ -499,10 +521,10 @@ static void strong_form_con_eq_T(const prm_t *p, double WiN, gp_t *g)
 /* Constitutive_Models_SQRT_mod.F90                                        */
 
 /* WTensor2D :513-530 with omegaNominator2DReal :534-543, omegaDenominator2DReal :575-584 */
-static void wtensor2d(const double S[2][2], const double GUT[2][2], double W[2][2])
+static void wtensor2d(const real_t S[2][2], const real_t GUT[2][2], real_t W[2][2])
 {
-    double n = -S[0][0] * GUT[1][0] + S[0][1] * (GUT[0][0] - GUT[1][1]) + S[1][1] * GUT[0][1];
-    double d = S[0][0] + S[1][1];
+    real_t n = -S[0][0] * GUT[1][0] + S[0][1] * (GUT[0][0] - GUT[1][1]) + S[1][1] * GUT[0][1];
+    real_t d = S[0][0] + S[1][1];
     W[0][0] = 0.0;
     W[1][1] = 0.0;
     W[0][1] = n / d;
@@ -510,9 +532,9 @@ static void wtensor2d(const double S[2][2], const double GUT[2][2], double W[2][
 }
 
 /* setOmegaTensor :420-455 */
-static void omega_tensor(const double S3[3][3], const double GUT3[3][3], double W[3][3])
+static void omega_tensor(const real_t S3[3][3], const real_t GUT3[3][3], real_t W[3][3])
 {
-    double s[2][2], gt[2][2], w[2][2];
+    real_t s[2][2], gt[2][2], w[2][2];
     for (int i = 0; i < 2; i++)
         for (int j = 0; j < 2; j++) {
             s[i][j] = S3[i][j];
@@ -528,9 +550,9 @@ static void omega_tensor(const double S3[3][3], const double GUT3[3][3], double 
 /* conEQ_*_SQRT :153-375 */
 static void con_eq_sqrt(const prm_t *p, gp_t *g)
 {
-    const double N = (double)NDIM;
+    const real_t N = (real_t)NDIM;
     double VeN = p->VeN;
-    double trC = trace3(g->C_Tensor);
+    real_t trC = trace3(g->C_Tensor);
     for (int a = 0; a < 2; a++)
         for (int c = 0; c < 3; c++) g->dgdxi[a][c] = 0.0;
     switch (p->model) {
@@ -549,12 +571,12 @@ static void con_eq_sqrt(const prm_t *p, gp_t *g)
         for (int c = 0; c < 3; c++) g->dgdxi[1][c] = g->dgdxi[0][c];
         break;
     case M_E_PTT:
-        g->f_T = exp(VeN * (trC - N));
+        g->f_T = REXP(VeN * (trC - N));
         g->f[0] = g->f_T; g->f[1] = g->f[0]; g->f[2] = 0.0;
         g->g[0] = 1.0; g->g[1] = 1.0;
         break;
     case M_M_E_PTT:
-        g->f_T = exp(VeN * (trC - N));
+        g->f_T = REXP(VeN * (trC - N));
         g->f[0] = g->f_T; g->f[1] = g->f[0]; g->f[2] = 0.0;
         g->g[0] = g->f_T; g->g[1] = g->f_T;
         for (int i = 0; i < 3; i++)
@@ -592,7 +614,7 @@ static void set_c_tensor_sqrt(gp_t *g)
 {
     matmul3(g->S, g->S, g->C_Tensor);
     for (int k = 0; k < 3; k++) {
-        double dS[3][3], A[3][3], B[3][3];
+        real_t dS[3][3], A[3][3], B[3][3];
         for (int i = 0; i < 3; i++)
             for (int j = 0; j < 3; j++) dS[i][j] = g->dSdXi[i][j][k];
         matmul3(dS, g->S, A);
@@ -603,7 +625,7 @@ static void set_c_tensor_sqrt(gp_t *g)
 }
 
 /* setStressTensorSQRT :483-509 */
-static void set_stress_tensor_sqrt(const prm_t *p, double WiN, gp_t *g)
+static void set_stress_tensor_sqrt(const prm_t *p, real_t WiN, gp_t *g)
 {
     double BvN = p->BvN;
     for (int i = 0; i < 3; i++)
@@ -628,13 +650,13 @@ static void set_stress_tensor_sqrt(const prm_t *p, double WiN, gp_t *g)
 
 /* strongFormConEQ_SQRT :120-149, setUpperConvectedDerivativeSQRT :397-416,
  * setSInverse :459-479 */
-static void strong_form_con_eq_sqrt(const prm_t *p, double WiN, gp_t *g)
+static void strong_form_con_eq_sqrt(const prm_t *p, real_t WiN, gp_t *g)
 {
     set_c_tensor_sqrt(g);
     con_eq_sqrt(p, g);
     set_stress_tensor_sqrt(p, WiN, g);
 
-    double UCD[3][3], W[3][3], M1[3][3], M2[3][3];
+    real_t UCD[3][3], W[3][3], M1[3][3], M2[3][3];
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++) UCD[i][j] = g->dSdt[i][j];
     for (int k = 0; k < 3; k++)
@@ -647,7 +669,7 @@ static void strong_form_con_eq_sqrt(const prm_t *p, double WiN, gp_t *g)
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++) UCD[i][j] = UCD[i][j] - M1[i][j] - M2[i][j];
 
-    double s2[2][2], si2[2][2], SI[3][3], SS[3][3], S3[3][3];
+    real_t s2[2][2], si2[2][2], SI[3][3], SS[3][3], S3[3][3];
     for (int i = 0; i < 2; i++)
         for (int j = 0; j < 2; j++) s2[i][j] = g->S[i][j];
     inverse2(s2, si2);
@@ -659,7 +681,7 @@ static void strong_form_con_eq_sqrt(const prm_t *p, double WiN, gp_t *g)
     matmul3(g->S, SS, S3);
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++) {
-            double term = (g->f[2]) * S3[i][j] + (g->f[1]) * g->S[i][j] - (g->f[0]) * SI[i][j];
+            real_t term = (g->f[2]) * S3[i][j] + (g->f[1]) * g->S[i][j] - (g->f[0]) * SI[i][j];
             g->Con_EQ[i][j] = WiN * UCD[i][j] + term / 2.0;
         }
 }
@@ -667,14 +689,14 @@ static void strong_form_con_eq_sqrt(const prm_t *p, double WiN, gp_t *g)
 /* strongFormMomentum :658-683 */
 static void strong_form_momentum(const prm_t *p, gp_t *g)
 {
-    double div_Tve[3] = {0.0, 0.0, 0.0}, div_Ptot[3];
+    real_t div_Tve[3] = {0.0, 0.0, 0.0}, div_Ptot[3];
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++) div_Tve[i] = div_Tve[i] + g->dTdXi[j][i][j];
     for (int i = 0; i < 3; i++)
         div_Ptot[i] = -g->dPdXi[i] + div_Tve[i]
                       + p->BvN * (g->G2U[0][i] + g->G2U[1][i] + g->G2U[2][i]);
     for (int i = 0; i < 3; i++) {
-        double s = 0.0;
+        real_t s = 0.0;
         for (int k = 0; k < 3; k++) s = s + g->U_f[k] * g->GU[k][i];
         g->Convection[i] = g->dUfdt[i] + s;
     }
@@ -682,9 +704,9 @@ static void strong_form_momentum(const prm_t *p, gp_t *g)
 }
 
 /* setContinuationParameter :577-601, strongFormEquations :537-573 */
-static double strong_form_equations(const prm_t *p, const elem_t *E, gp_t *g)
+static real_t strong_form_equations(const prm_t *p, const elem_t *E, gp_t *g)
 {
-    double WiN = p->WiN;
+    real_t WiN = p->WiN;
     if (p->nex > 0) WiN = p->Wi0 * E->eu[p->nex - 1];
     set_flow_kinematics(g);
     for (int i = 0; i < 3; i++) {
@@ -701,30 +723,30 @@ static double strong_form_equations(const prm_t *p, const elem_t *E, gp_t *g)
 }
 
 /* setStabilizationTerms :701-773 */
-static void set_stabilization_terms(const prm_t *p, double WiN, const elem_t *E, gp_t *g)
+static void set_stabilization_terms(const prm_t *p, real_t WiN, const elem_t *E, gp_t *g)
 {
     double BvN = p->BvN, ReN = p->ReN, DfN = p->DfN, dt = p->dt;
-    double Helem = 0.0, tsugn = 0.0;
+    real_t Helem = 0.0, tsugn = 0.0;
     for (int n = 0; n < NBF; n++) {
         Helem = Helem + E->dFdXi[0][n] * E->dFdXi[0][n] + E->dFdXi[1][n] * E->dFdXi[1][n]
                 + E->dFdXi[2][n] * E->dFdXi[2][n];
-        double dF[3] = {E->dFdXi[0][n], E->dFdXi[1][n], E->dFdXi[2][n]};
-        tsugn = tsugn + fabs(dot3(g->U_f, dF));
+        real_t dF[3] = {E->dFdXi[0][n], E->dFdXi[1][n], E->dFdXi[2][n]};
+        tsugn = tsugn + RABS(dot3(g->U_f, dF));
     }
-    Helem = 1.0 / sqrt(Helem);
+    Helem = 1.0 / RSQRT(Helem);
 
-    double double_dot_T = ddot3(g->T_ve, g->T_ve);
-    double double_dot_G = ddot3(g->G_dot_tr, g->G_dot_tr);
-    double Ha = sqrt(((1.0 - BvN) / WiN) * ((1.0 - BvN) / WiN) + 0.5 * double_dot_T);
-    Ha = Ha / sqrt(1.0 + 0.5 * double_dot_G);
+    real_t double_dot_T = ddot3(g->T_ve, g->T_ve);
+    real_t double_dot_G = ddot3(g->G_dot_tr, g->G_dot_tr);
+    real_t Ha = RSQRT(((1.0 - BvN) / WiN) * ((1.0 - BvN) / WiN) + 0.5 * double_dot_T);
+    Ha = Ha / RSQRT(1.0 + 0.5 * double_dot_G);
 
-    double H2 = Helem * Helem;
-    double t1 = ReN / dt, t2 = ReN * tsugn, t3 = BvN / H2, t4 = Ha / H2;
+    real_t H2 = Helem * Helem;
+    real_t t1 = ReN / dt, t2 = ReN * tsugn, t3 = BvN / H2, t4 = Ha / H2;
     g->tlsme = t1 * t1 + t2 * t2 + t3 * t3 + t4 * t4;
-    g->tlsme = 1.0 / sqrt(g->tlsme);
+    g->tlsme = 1.0 / RSQRT(g->tlsme);
     g->tlsic = H2 / (g->tlsme);
 
-    double double_dot_S = ddot3(g->S, g->S), double_dot_C;
+    real_t double_dot_S = ddot3(g->S, g->S), double_dot_C;
     g->tdcs = 0.5 * double_dot_S;
     if (p->form == FORM_SQRT) {
         double_dot_C = ddot3(g->C_Tensor, g->C_Tensor);
@@ -732,36 +754,36 @@ static void set_stabilization_terms(const prm_t *p, double WiN, const elem_t *E,
         g->tdcs = (g->tdcs) + ((1.0 - BvN) / WiN) * ((1.0 - BvN) / WiN);
         double_dot_C = double_dot_T;
     }
-    g->tdcs = H2 / sqrt(g->tdcs);
+    g->tdcs = H2 / RSQRT(g->tdcs);
     if (DfN > 1.0e-12) g->tdcs = 0.0;
 
     g->mag_con_EQ = ddot3(g->Con_EQ, g->Con_EQ);
-    g->mag_con_EQ = sqrt(0.5 * g->mag_con_EQ);
+    g->mag_con_EQ = RSQRT(0.5 * g->mag_con_EQ);
 
-    double s1 = WiN / dt, s2 = WiN * tsugn, s3 = WiN * sqrt(0.5 * double_dot_G), s4 = g->f[1];
-    double s5 = g->f[2] * sqrt(0.5 * double_dot_C), s6 = (g->tdcs) * (g->mag_con_EQ) / H2;
-    double s7 = DfN / H2;
+    real_t s1 = WiN / dt, s2 = WiN * tsugn, s3 = WiN * RSQRT(0.5 * double_dot_G), s4 = g->f[1];
+    real_t s5 = g->f[2] * RSQRT(0.5 * double_dot_C), s6 = (g->tdcs) * (g->mag_con_EQ) / H2;
+    real_t s7 = DfN / H2;
     g->tlsce = s1 * s1 + s2 * s2 + s3 * s3 + s4 * s4 + s5 * s5 + s6 * s6 + s7 * s7;
-    g->tlsce = 1.0 / sqrt(g->tlsce);
+    g->tlsce = 1.0 / RSQRT(g->tlsce);
 }
 
 /* ---------------------------------------------------------------------- */
 /* Residuals_mod.F90                                                       */
 
 /* momentumMain :44-86 (T) and momentumMainSQRT :295-337 with LSCEMomentumSQRT :388-433 */
-static void momentum_main(const prm_t *p, double WiN, const elem_t *E, int inod, const gp_t *g,
-                          double *res)
+static void momentum_main(const prm_t *p, real_t WiN, const elem_t *E, int inod, const gp_t *g,
+                          real_t *res)
 {
     double bifn = E->bfn[inod];
-    double dF[3] = {E->dFdXi[0][inod], E->dFdXi[1][inod], E->dFdXi[2][inod]};
+    real_t dF[3] = {E->dFdXi[0][inod], E->dFdXi[1][inod], E->dFdXi[2][inod]};
     for (int i = 0; i < NEQ_F; i++) {
-        double lsme_term = (g->tlsme) * p->ReN * dot3(g->U_f, dF);  /* LSMEMomentum :161-173 */
+        real_t lsme_term = (g->tlsme) * p->ReN * dot3(g->U_f, dF);  /* LSMEMomentum :161-173 */
         lsme_term = lsme_term * (g->Momentum[i]);
-        double lsic_term = g->tlsic * dF[i];                        /* LSICMomentum :177-187 */
+        real_t lsic_term = g->tlsic * dF[i];                        /* LSICMomentum :177-187 */
         lsic_term = lsic_term * (g->Continuity);
-        double lsce[3][3];
+        real_t lsce[3][3];
         if (p->form == FORM_SQRT) {
-            double GUT_lsce[3][3], GU_lsce[3][3], W_lsce[3][3], M1[3][3], M2[3][3];
+            real_t GUT_lsce[3][3], GU_lsce[3][3], W_lsce[3][3], M1[3][3], M2[3][3];
             for (int a = 0; a < 3; a++)
                 for (int b = 0; b < 3; b++) GUT_lsce[a][b] = 0.0;
             for (int b = 0; b < 3; b++) GUT_lsce[i][b] = dF[b];
@@ -772,54 +794,54 @@ static void momentum_main(const prm_t *p, double WiN, const elem_t *E, int inod,
             matmul3(W_lsce, g->S, M2);
             for (int a = 0; a < 3; a++)
                 for (int b = 0; b < 3; b++) {
-                    double ucd = -M1[a][b] - M2[a][b];
+                    real_t ucd = -M1[a][b] - M2[a][b];
                     lsce[a][b] = (g->tlsce) * ucd * (1.0 - p->BvN) / WiN;
                 }
         } else {                                                    /* LSCEMomentumT :191-219 */
             for (int a = 0; a < 3; a++)
                 for (int b = 0; b < 3; b++) lsce[a][b] = -g->tlsce * (a == i ? dF[b] : 0.0);
         }
-        double lsce_term = ddot3(lsce, g->Con_EQ);
-        double Pi[3] = {g->P_tot[i][0], g->P_tot[i][1], g->P_tot[i][2]};
+        real_t lsce_term = ddot3(lsce, g->Con_EQ);
+        real_t Pi[3] = {g->P_tot[i][0], g->P_tot[i][1], g->P_tot[i][2]};
         res[i] = p->ReN * (g->Convection[i]) * bifn + dot3(Pi, dF) + lsme_term + lsic_term
                  + lsce_term;
     }
 }
 
 /* continuityBulkMain :90-110 with LSMEContinuity :223-234 */
-static void continuity_main(const elem_t *E, int inod, const gp_t *g, double *res)
+static void continuity_main(const elem_t *E, int inod, const gp_t *g, real_t *res)
 {
     double bifn = E->bfn[inod];
-    double dF[3] = {E->dFdXi[0][inod], E->dFdXi[1][inod], E->dFdXi[2][inod]};
-    double lsme_term = g->tlsme * dot3(dF, g->Momentum);
+    real_t dF[3] = {E->dFdXi[0][inod], E->dFdXi[1][inod], E->dFdXi[2][inod]};
+    real_t lsme_term = g->tlsme * dot3(dF, g->Momentum);
     res[NEQ_F] = (g->Continuity) * bifn + lsme_term;
 }
 
 /* stressesBulkMain :114-157 (T) and stressesBulkMainSQRT :341-384 */
-static void stresses_main(const prm_t *p, double WiN, const elem_t *E, int inod, const gp_t *g,
-                          double *res)
+static void stresses_main(const prm_t *p, real_t WiN, const elem_t *E, int inod, const gp_t *g,
+                          real_t *res)
 {
     double bifn = E->bfn[inod];
-    double dF[3] = {E->dFdXi[0][inod], E->dFdXi[1][inod], E->dFdXi[2][inod]};
+    real_t dF[3] = {E->dFdXi[0][inod], E->dFdXi[1][inod], E->dFdXi[2][inod]};
     int istart = NEQ - NEQ_S;
     for (int i = istart; i < NEQ; i++) {
         int j, k;
         stress_component(i, istart, &j, &k);
         /* LSMEStressT :238-256 / LSMEStressSQRT :437-455 */
-        double lsme_term = -dF[k] * g->Momentum[j];
+        real_t lsme_term = -dF[k] * g->Momentum[j];
         if (j != k) lsme_term = lsme_term - dF[j] * g->Momentum[k];
         if (p->form == FORM_SQRT)
             lsme_term = (g->tlsme) * lsme_term * WiN;
         else
             lsme_term = g->tlsme * lsme_term * (1.0 - p->BvN);
         /* LSCEStressT :260-276 / LSCEStressSQRT :459-475 */
-        double lsce_term = WiN * dot3(g->U_f, dF);
+        real_t lsce_term = WiN * dot3(g->U_f, dF);
         if (p->form == FORM_SQRT) lsce_term = lsce_term + (g->f_T) * bifn / 2.0;
         lsce_term = (g->tlsce) * lsce_term;
         lsce_term = lsce_term * (g->Con_EQ[j][k]);
         /* DCSStressT :280-291 / DCSStressSQRT :479-490 */
-        const double *grad = (p->form == FORM_SQRT) ? g->dSdXi[j][k] : g->dTdXi[j][k];
-        double dcs_term = (g->tdcs) * dot3(grad, dF);
+        const real_t *grad = (p->form == FORM_SQRT) ? g->dSdXi[j][k] : g->dTdXi[j][k];
+        real_t dcs_term = (g->tdcs) * dot3(grad, dF);
         dcs_term = dcs_term * (g->mag_con_EQ);
         res[i] = (g->Con_EQ[j][k]) * bifn + p->DfN * dot3(grad, dF) + lsme_term + lsce_term
                  + dcs_term;
@@ -830,7 +852,7 @@ static void stresses_main(const prm_t *p, double WiN, const elem_t *E, int inod,
 /* Equations_mod.F90                                                       */
 
 /* residualBulk :59-98 with equationsResidualsBulkMain :102-144 */
-static void residual_bulk(const prm_t *p, const gauss_t *G, elem_t *E, double Res[NBF][NEQ])
+static void residual_bulk(const prm_t *p, const gauss_t *G, elem_t *E, real_t Res[NBF][NEQ])
 {
     gp_t g;
     memset(&g, 0, sizeof(g));
@@ -840,11 +862,11 @@ static void residual_bulk(const prm_t *p, const gauss_t *G, elem_t *E, double Re
         set_element_basis(G, ig, E);
         basis2d(E, &g);
         set_flow_unknowns(E, &g);                      /* setFlowQuantities :247-262 */
-        double WiN = strong_form_equations(p, E, &g);
+        real_t WiN = strong_form_equations(p, E, &g);
         set_stabilization_terms(p, WiN, E, &g);
         g.WET = (G->w[ig]) * fabs(g.detJ);
         for (int inod = 0; inod < NBF; inod++) {
-            double term[NEQ];
+            real_t term[NEQ];
             for (int e = 0; e < NEQ; e++) term[e] = 0.0;
             momentum_main(p, WiN, E, inod, &g, term);
             continuity_main(E, inod, &g, term);
@@ -858,14 +880,14 @@ static void residual_bulk(const prm_t *p, const gauss_t *G, elem_t *E, double Re
  * The perturbation is restored by subtraction (x + eps) - eps exactly as the
  * Fortran does (:272, :276), so rounding residue carries into later columns. */
 static void store_bulk(const prm_t *p, const gauss_t *G, elem_t *E, int want_jac,
-                       double Res[NBF][NEQ], double *A /* [9][6][9][6] */, double *Ac /* [9][6][nex] */)
+                       real_t Res[NBF][NEQ], real_t *A /* [9][6][9][6] */, real_t *Ac /* [9][6][nex] */)
 {
     residual_bulk(p, G, E, Res);
     if (!want_jac) return;
-    double dRes[NBF][NEQ];
+    real_t dRes[NBF][NEQ];
     for (int inod = 0; inod < NBF; inod++) {
         for (int ieq = 0; ieq < NEQ; ieq++) {
-            double eps_jac = p->eps; /* perturbVariableReal, Tools_mod.F90:831-840 */
+            real_t eps_jac = p->eps; /* perturbVariableReal, Tools_mod.F90:831-840 */
             E->tl[inod][ieq] = E->tl[inod][ieq] + eps_jac;
             residual_bulk(p, G, E, dRes);
             E->tl[inod][ieq] = E->tl[inod][ieq] - eps_jac;
@@ -876,7 +898,7 @@ static void store_bulk(const prm_t *p, const gauss_t *G, elem_t *E, int want_jac
         }
     }
     for (int inex = 0; inex < p->nex; inex++) {
-        double eps_jac = p->eps;
+        real_t eps_jac = p->eps;
         E->eu[inex] = E->eu[inex] + eps_jac;
         residual_bulk(p, G, E, dRes);
         E->eu[inex] = E->eu[inex] - eps_jac;
@@ -886,6 +908,7 @@ static void store_bulk(const prm_t *p, const gauss_t *G, elem_t *E, int want_jac
     }
 }
 
+#ifndef ORA_COMPLEX_STEP
 /* ---------------------------------------------------------------------- */
 /* C interface for the tests (ctypes)                                      */
 
@@ -1138,3 +1161,77 @@ int ora_gp_probe(const int *ip, const double *dp, int nel, int nnodes, const int
     }
     return 0;
 }
+#endif /* !ORA_COMPLEX_STEP */
+
+#ifdef ORA_COMPLEX_STEP
+static void cs_unpack_params(const int *ip, const double *dp, prm_t *p)
+{
+    p->model = ip[0];
+    p->form = ip[1];
+    p->nex = ip[2];
+    p->ReN = dp[0];
+    p->WiN = dp[1];
+    p->BvN = dp[2];
+    p->VeN = dp[3];
+    p->DfN = dp[4];
+    p->Wi0 = dp[5];
+    p->dt = dp[6];
+    p->eps = dp[7];
+}
+
+/* Exact element Jacobians by the complex step, elements [e0, e1), in the
+ * layouts of ora_element_batch: res[e][9][6], jac[e][9][6][9][6]
+ * (d Res(jnod,jeq) / d TL(inod,ieq) at [inod][ieq][jnod][jeq]) and
+ * ac[e][9][6][nex] (d Res(inod,ieq) / d EU(inex)). */
+int ora_cs_element_batch(const int *ip, const double *dp, int nel, int nnodes, const int *conn,
+                         const double *xyz, const double *TL, const double *EU, int e0, int e1,
+                         double *res, double *jac, double *ac, int nthreads)
+{
+    const double h = 1.0e-30;
+    prm_t p;
+    cs_unpack_params(ip, dp, &p);
+    gauss_t G;
+    gauss_tables(&G);
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 4)
+#endif
+    for (int iel = e0; iel < e1; iel++) {
+        elem_t E;
+        real_t Res[NBF][NEQ], dRes[NBF][NEQ];
+        memset(&E, 0, sizeof(E));
+        for (int inod = 0; inod < NBF; inod++) {
+            int g = conn[inod * nel + iel] - 1;
+            for (int ieq = 0; ieq < NEQ; ieq++) E.tl[inod][ieq] = TL[(size_t)ieq * nnodes + g];
+            for (int j = 0; j < 3; j++) E.xi[inod][j] = xyz[(size_t)j * nnodes + g];
+        }
+        for (int i = 0; i < p.nex; i++) E.eu[i] = EU[i];
+        size_t k = (size_t)(iel - e0);
+        residual_bulk(&p, &G, &E, Res);
+        for (int inod = 0; inod < NBF; inod++)
+            for (int ieq = 0; ieq < NEQ; ieq++) res[k * 54 + inod * NEQ + ieq] = creal(Res[inod][ieq]);
+        for (int inod = 0; inod < NBF; inod++)
+            for (int ieq = 0; ieq < NEQ; ieq++) {
+                const double x0 = creal(E.tl[inod][ieq]);
+                E.tl[inod][ieq] = CMPLX(x0, h);
+                residual_bulk(&p, &G, &E, dRes);
+                E.tl[inod][ieq] = x0;
+                for (int jnod = 0; jnod < NBF; jnod++)
+                    for (int jeq = 0; jeq < NEQ; jeq++)
+                        jac[k * 2916 + ((inod * NEQ + ieq) * NBF + jnod) * NEQ + jeq] =
+                            cimag(dRes[jnod][jeq]) / h;
+            }
+        for (int inex = 0; inex < p.nex; inex++) {
+            const double x0 = creal(E.eu[inex]);
+            E.eu[inex] = CMPLX(x0, h);
+            residual_bulk(&p, &G, &E, dRes);
+            E.eu[inex] = x0;
+            for (int inod = 0; inod < NBF; inod++)
+                for (int ieq = 0; ieq < NEQ; ieq++)
+                    ac[(k * 54 + inod * NEQ + ieq) * p.nex + inex] = cimag(dRes[inod][ieq]) / h;
+        }
+    }
+    (void)nthreads;
+    return 0;
+}
+#endif /* ORA_COMPLEX_STEP */
