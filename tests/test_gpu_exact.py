@@ -141,7 +141,10 @@ MODELS7 = [("L-PTT", 0.05), ("m-L-PTT", 0.05), ("e-PTT", 0.05), ("m-e-PTT", 0.05
 def test_exact64_matches_complex_step_oracle_2000(model, ve, form):
     """FP64 exact Jacobian on the 2,000-quad cylinder mesh against the
     oracle's complex-step Jacobian: <= 1e-12 relative (max-norm of the
-    difference over max-norm of the matrix), every model and both forms."""
+    difference over max-norm of the matrix), every model and both forms.
+    The residual is bit-identical, except for the exponential-PTT models
+    (1e-12 relative: exp() of the host and of CUDA may differ in the last
+    bit)."""
     mesh = M.build_cylinder_mesh(2000)
     phys = S.Physics(model=model, form=form, WiN=0.3, Wi0=0.3, BvN=0.59, VeN=ve, nex=1)
     TL, EU = S.seeded_state(mesh.xyz, phys, 5)
@@ -150,7 +153,11 @@ def test_exact64_matches_complex_step_oracle_2000(model, ve, form):
     b, v64 = asm.set_equations_bulk(TL, EU, "NRP", jacobian="exact64")
     asm.close()
     bo, vo = O.exact_assemble(phys, mesh.conn, mesh.xyz, TL, EU, rowptr, colind)
-    assert np.array_equal(b, bo)
+    if model in ("e-PTT", "m-e-PTT"):
+        # host libm and CUDA exp() may differ in the last bit
+        assert np.max(np.abs(b - bo)) <= 1e-12 * np.max(np.abs(bo))
+    else:
+        assert np.array_equal(b, bo)
     assert np.max(np.abs(v64 - vo)) <= 1e-12 * np.max(np.abs(vo))
 
 
