@@ -85,9 +85,15 @@ def parse_args():
     ap.add_argument("--cont-arms", default="",
                     help="comma-separated arm names of the continuation comparison to run "
                          "(default: all)")
+    ap.add_argument("--newton-nel", type=int, default=40000,
+                    help="mesh of the precision-form Newton comparison in the default line "
+                         "(0 = skip it)")
     ap.add_argument("--newton-only", type=int, default=0, metavar="NEL",
                     help="only the precision-form Newton comparison (FP64 vs FP32 Jacobian, "
                          "natural continuation Wi 0.1, 0.3, 0.5) on a mesh of NEL quads")
+    ap.add_argument("--linear-solver", choices=["auto", "frontal", "superlu"], default="auto",
+                    help="linear solver of the Newton and continuation legs (auto: the GPU "
+                         "frontal LU from 1,000 elements on, host SuperLU below)")
     ap.add_argument("--continuation-only", action="store_true",
                     help="run only the continuation comparison and print its JSON line")
     ap.add_argument("--batch-inst", type=int, default=64,
@@ -216,6 +222,26 @@ def fp64_peak(device: int):
     return {"dfma_inst_per_s": out[0], "dadd_inst_per_s": out[1], "dmul_inst_per_s": out[2]}
 
 
+def measured_hbm_gbs():
+    """The machine's measured copy bandwidth (GB/s), if the file is present."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def fp32_peak(device: int) -> float:
+    """FFMA instructions/s of a probe kernel on this GPU."""
+    lib = ctypes.CDLL(B.PROBE)
+    lib.vefem_probe_fp32.argtypes = [ctypes.c_int, ctypes.c_void_p]
+    out = np.zeros(1)
+    rc = lib.vefem_probe_fp32(device, out.ctypes.data)
+    if rc:
+        raise RuntimeError(f"FP32 probe failed: {rc}")
+    return float(out[0])
+
+
 def algorithmic_ops(phys, flags):
     L = V.load()
     L.vefem_algorithmic_ops.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
@@ -297,7 +323,7 @@ def run_reference(args):
 
 def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=None,
                          secant: bool = True, step_log=None, ablations: bool = True,
-                         only=None):
+                         only=None, linear_solver: str = "auto"):
     """Arclength continuation Wi 0.1 -> wi_end (Oldroyd-B, beta = 0.59, SQRT
     form) on the GPU assembly, arms from the same start: the plain FP64 path
     (FD64 Jacobian, the reference's tangent predictor), the same with a
@@ -309,15 +335,22 @@ def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=Non
     arm with the reference's factorisation-reuse rules, and the contraction
     policy without the network (the reduced-space extrapolation alone).
     Every point is converged to ||R|| < 1e-10 and ||dx|| < 1e-10; host wall
-    time per arm."""
+    time per arm.  All arms share one linear solver (``linear_solver``: the
+    GPU frontal LU, or the host SuperLU on small meshes), whose one-time
+    symbolic phase is timed apart."""
     from ve_flow_around_cylinder_fortran_gb300 import continuation as C
     from ve_flow_around_cylinder_fortran_gb300 import learned as LP
+    from ve_flow_around_cylinder_fortran_gb300 import linsolve as LS
     from ve_flow_around_cylinder_fortran_gb300 import newton as NW
     mesh = M.build_cylinder_mesh(nel)
     phys = S.oldroyd_b(0.1, 0.59, "SQRT", nex=1)
     TL, EU = NW.initial_state(mesh, phys)
     rowptr, colind = P.build_pattern(mesh.element_nodes(), mesh.nnodes, phys.nex)
     asm = V.BulkAssembler(mesh, phys, rowptr, colind, outlet_edges=True, device=device)
+    t_sym = time.perf_counter()
+    solver = LS.make_solver(linear_solver, rowptr, colind, mesh)
+    t_sym = time.perf_counter() - t_sym
+    solver_name = type(solver).__name__
     cfg = C.ArclengthSettings(dArN=0.01, lam_max=wi_end / phys.Wi0, max_steps=2000)
     # the learned + mixed arm reuses factorisations across steps while chord
     # iterations contract (theta < 0.6) and cuts a failed step back (dS halved,
@@ -334,7 +367,8 @@ def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=Non
     if only:
         runs = [r for r in runs if r[0] in only]
     for name, jac, kind, arm_cfg in runs:
-        cont = C.ArclengthContinuation(asm, mesh, phys, jac, arm_cfg, log=step_log)
+        cont = C.ArclengthContinuation(asm, mesh, phys, jac, arm_cfg, log=step_log,
+                                       linear_solver=solver)
         if step_log:
             step_log(f"arm {name}")
         pred = None
@@ -381,7 +415,8 @@ def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=Non
     out = {
         "workload": f"arclength continuation Wi 0.1 -> {wi_end}, Oldroyd-B beta=0.59, SQRT form, "
                     f"{mesh.nel} Q2 quads ({len(rowptr) - 1} unknowns), LN0=1, dArN=0.01, "
-                    "Eps_Pr=1e-3, dS0=1, dS_max=50; host SuperLU (nested dissection) solve",
+                    f"Eps_Pr=1e-3, dS0=1, dS_max=50; linear solver: {_solver_desc(solver)}",
+        "linear_solver": solver_name, "solver_setup_s": t_sym,
         "arms": arms,
     }
     if "plain_fp64" not in states or "learned_fp32" not in states:
@@ -405,7 +440,15 @@ def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=Non
     return out
 
 
-def newton_precision_compare(nel: int, device: int = 0, wis=(0.1, 0.3, 0.5)):
+def _solver_desc(solver) -> str:
+    if type(solver).__name__ == "FrontalLU":
+        return (f"GPU panel-frontal LU, FP64 ({solver.npan} panels of {solver.G} elements, "
+                f"{solver.flops / 1e12:.2f} TFLOP per factorisation)")
+    return "host SuperLU (nested dissection)"
+
+
+def newton_precision_compare(nel: int, device: int = 0, wis=(0.1, 0.3, 0.5),
+                             linear_solver: str = "auto"):
     """Precision form on one Newton solve per Weissenberg number: Giesekus
     alpha = 0.1, beta = 0.59, SQRT form, natural continuation through ``wis``
     from the fully developed start, each point to ||R|| < 1e-10 and
@@ -414,15 +457,20 @@ def newton_precision_compare(nel: int, device: int = 0, wis=(0.1, 0.3, 0.5)):
     bit) and once with the FP32 exact Jacobian beside the FP64 residual.
     Reports iterations, factorisations and host time per solve, and the FP32
     run's converged state against the FP64 one."""
+    from ve_flow_around_cylinder_fortran_gb300 import linsolve as LS
     from ve_flow_around_cylinder_fortran_gb300 import newton as NW
     mesh = M.build_cylinder_mesh(nel)
     phys = S.giesekus(0.1, wis[0], 0.59, "SQRT", nex=0)
     rowptr, colind = P.build_pattern(mesh.element_nodes(), mesh.nnodes, phys.nex)
     asm = V.BulkAssembler(mesh, phys, rowptr, colind, outlet_edges=True, device=device)
+    t_sym = time.perf_counter()
+    solver = LS.make_solver(linear_solver, rowptr, colind, mesh)
+    t_sym = time.perf_counter() - t_sym
     runs, final = {}, {}
     for jac in ("fd64", "exact32"):
         t0 = time.perf_counter()
-        res = NW.natural_continuation(asm, mesh, phys, list(wis), jacobian=jac, tol=1e-10)
+        res = NW.natural_continuation(asm, mesh, phys, list(wis), jacobian=jac, tol=1e-10,
+                                      linear_solver=solver)
         wall = time.perf_counter() - t0
         runs[jac] = {
             "wall_s": wall,
@@ -439,7 +487,8 @@ def newton_precision_compare(nel: int, device: int = 0, wis=(0.1, 0.3, 0.5)):
         "workload": f"Newton solves by natural continuation Wi = {', '.join(str(w) for w in wis)}, "
                     f"Giesekus alpha=0.1, beta=0.59, SQRT form, {mesh.nel} Q2 quads "
                     f"({len(rowptr) - 1} unknowns), outlet edges, Dirichlet rows on the device; "
-                    "host SuperLU (nested dissection)",
+                    f"linear solver: {_solver_desc(solver)}",
+        "linear_solver": type(solver).__name__, "solver_setup_s": t_sym,
         "fd64": runs["fd64"], "fp32_jacobian": runs["exact32"],
         "solution_rel_err_2norm": float(np.linalg.norm(d) / np.linalg.norm(final["fd64"])),
         "solution_rel_err_maxnorm": float(np.max(np.abs(d)) / np.max(np.abs(final["fd64"]))),
@@ -608,7 +657,8 @@ def run_vefem(args):
         return 0
     if args.newton_only > 0:
         if rank == 0:
-            print(json.dumps({"newton_precision": newton_precision_compare(args.newton_only, dev)}))
+            print(json.dumps({"newton_precision": newton_precision_compare(
+                args.newton_only, dev, linear_solver=args.linear_solver)}))
         return 0
     if args.continuation_only:
         if rank == 0:
@@ -616,6 +666,7 @@ def run_vefem(args):
                 args.cont_nel, args.cont_wi, dev, secant=not args.no_secant,
                 ablations=not args.no_ablations,
                 only=[a for a in args.cont_arms.split(",") if a] or None,
+                linear_solver=args.linear_solver,
                 step_log=(lambda m: print(m, file=sys.stderr, flush=True)) if args.cont_log else None)
             print(json.dumps({"continuation": out}))
         if dist:
@@ -699,6 +750,38 @@ def run_vefem(args):
                        "scatter_ms": statistics.mean(x[1] + x[2] for x in tk),
                        "residual": "FP64 (bit-exact)",
                        "jacobian": "exact derivative, " + ("FP32" if "32" in name else "FP64")}
+    # ---- roofline of the precision form's Jacobian kernel alone (no residual
+    #      beside it): FP32 operations counted from its source / its event time,
+    #      against the FFMA rate of a probe kernel (an FMA = two operations)
+    jflags = V.VEFEM_JAC_EXACT32 | V.VEFEM_ZERO_FIRST | V.VEFEM_TIMING
+    for _ in range(args.warmup):
+        asm.assemble(tTL, tEU, jflags, None, tv32, on_device=True)
+    torch.cuda.synchronize()
+    jk = []
+    for _ in range(args.steps):
+        asm.assemble(tTL, tEU, jflags, None, tv32, on_device=True)
+        jk.append(asm.last_timing()[0])
+    ops32 = algorithmic_ops(phys, V.VEFEM_JAC_EXACT32)
+    jk_ms = statistics.mean(jk)
+    ffma = fp32_peak(dev)
+    ach32 = ops32[0] * nel / (jk_ms * 1e-3)
+    step32 = forms["fp32_jacobian"]["ms_per_step"]
+    # algorithmic bytes of one precision-form step: state, coordinates and
+    # connectivity read, residual (FP64) and AIJ values (FP32) written
+    alg_bytes = (TL.nbytes + EU.nbytes + mesh.xyz[:2].nbytes + mesh.conn.nbytes
+                 + asm.N * 8 + asm.nnz * 4)
+    hbm = measured_hbm_gbs()
+    forms["fp32_jacobian"]["roofline"] = {
+        "kernel": "k_exact_batched<float>", "bound": "fp32", "achieved": ach32 / 1e12,
+        "peak": 2.0 * ffma / 1e12, "unit": "TOP/s", "frac": ach32 / (2.0 * ffma),
+        "traffic": None, "ops_per_element": ops32[0],
+        "ops_split": {"add": ops32[1], "mul": ops32[2], "div": ops32[3], "sqrt": ops32[4]},
+        "kernel_ms_avg": jk_ms,
+        "peak_source": "measured live: FFMA instruction rate of a probe kernel x 2",
+        "step_hbm": {"algorithmic_bytes": alg_bytes,
+                     "achieved_gbs": alg_bytes / (step32 * 1e-3) / 1e9,
+                     "peak_gbs": hbm, "frac": (alg_bytes / (step32 * 1e-3) / 1e9 / hbm) if hbm else None,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if hbm else None}}
     del tv32
 
     # ---- end to end through the C ABI with pinned host buffers
@@ -753,6 +836,9 @@ def run_vefem(args):
     asm.close()
     if world == 1 and args.batch_inst > 0:
         line["batched"] = batched_compare(args.batch_inst, max(3, args.steps // 2), args.warmup, dev)
+    if world == 1 and args.newton_nel > 0:
+        line["newton_precision"] = newton_precision_compare(args.newton_nel, dev,
+                                                            linear_solver=args.linear_solver)
     if world == 1 and args.cont_nel > 0:
         line["continuation"] = continuation_compare(args.cont_nel, args.cont_wi, dev,
                                                     secant=not args.no_secant,

@@ -46,6 +46,7 @@ extern "C" {
 #define VEFEM_ERR_CUDA 3         /* CUDA runtime error (text in vefem_last_error) */
 #define VEFEM_ERR_NOMEM 4        /* host or device allocation failed */
 #define VEFEM_ERR_UNSUPPORTED 5  /* option not available in this build */
+#define VEFEM_ERR_SINGULAR 6     /* vefem_frontal_factor: a pivot below the tolerance */
 
 /* constitutive models, in the order of setConEQ_T / setConEQ_SQRT
  * (Constitutive_Models_mod.F90:31-49, Constitutive_Models_SQRT_mod.F90:66-84) */
@@ -201,6 +202,42 @@ int vefem_assemble_residual_noalloc(const vefem_params *params, int nnodes, int 
                                     const double *EU, double *b, void *stream);
 
 int vefem_abi_version(void);
+
+/* ---- Linear solver: panel-frontal elimination on the device ----------------
+ * The numeric phases of the Newton drivers' direct solve, in place of the
+ * MUMPS factorisation and solve behind KSPSolve (Petsc_mod.F90:850; the
+ * bordered matrix of the arclength continuation, Extra_Equations_mod.F90:
+ * 698-829, included).  The symbolic phase is the caller's (the package's
+ * frontal.py): npan frontal matrices, panel q's n[q] x n[q] matrix row-major at
+ * buf + off[q], its p[q] pivots first and its front after them; idx
+ * [idx_off[q] .. idx_off[q+1]) the global unknown of every row/column of panel
+ * q (device, int64); ext [ext_off[q] ..) the position in panel q+1 of each
+ * front unknown of panel q (device, int32).  Every unknown is a pivot of
+ * exactly one panel (the p[q] sum to N).  The device arrays are the caller's
+ * and must outlive the handle.
+ * vefem_frontal_factor: buf holds the assembled original entries of every
+ * panel (zeros elsewhere); the elimination (blocked Gauss-Jordan without
+ * pivoting, with the Schur complement of each panel added into the next one)
+ * overwrites it with the factors.  Returns VEFEM_ERR_SINGULAR when a pivot is
+ * at most tol times the largest entry of its 16 x 16 pivot block (the caller
+ * then factorises with pivoting); min_pivot (may be NULL) receives the
+ * smallest such ratio.  Synchronises the stream.
+ * vefem_frontal_solve: x = A^-1 b with the factors in buf; b and x are device
+ * vectors of N doubles (b is not modified).  The sweeps are captured once per
+ * buf into a CUDA graph and replayed; asynchronous on the stream.
+ * stream: a cudaStream_t (NULL = default stream). */
+typedef struct vefem_frontal vefem_frontal;
+
+int vefem_frontal_create(int device, int npan, const int64_t *off, const int32_t *n,
+                         const int32_t *p, const int32_t *ext, const int64_t *ext_off,
+                         const int64_t *idx, const int64_t *idx_off, int64_t N,
+                         vefem_frontal **out);
+int vefem_frontal_factor(vefem_frontal *f, double *buf, void *stream, double tol,
+                         double *min_pivot);
+int vefem_frontal_solve(vefem_frontal *f, const double *buf, const double *b, double *x,
+                        void *stream);
+void vefem_frontal_destroy(vefem_frontal *f);
+const char *vefem_frontal_last_error(const vefem_frontal *f);
 
 /* ---- Linear stability: batched A/B assembly --------------------------------
  * setEquationsBulkStability (Stability/Equations_Stability_mod.F90:20-226):

@@ -72,8 +72,11 @@ def test_batched_equals_single(jac):
         b, v = _single(inst, flags, f32)
         assert np.array_equal(bb[k], b), k
         assert np.array_equal(vv[k], v), k
-    # graph replay on the same buffers gives the same bits
+    # graph replay on the same buffers, filled with garbage first, gives the
+    # same bits (VEFEM_ZERO_FIRST clears every entry, the lambda row included)
     info0 = bt.info()
+    for x in list(bufs[2]) + list(bufs[3]):
+        x.fill_(7.0)
     bt.assemble(*bufs[:2], flags, bufs[2], bufs[3], on_device=True)
     assert bt.info()["replays"] == info0["replays"] + 1
     for k in range(len(insts)):

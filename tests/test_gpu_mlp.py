@@ -56,6 +56,18 @@ def test_forward_matches_oracle():
     net.close()
 
 
+def test_loss_and_gradient_reproducible():
+    """The loss is reduced in a fixed order (no atomics): two evaluations on
+    the same data give the same bits, loss and gradient."""
+    net, _ = _pair(11)
+    X, T = _problem(300, 2)
+    l1, g1 = net.loss_grad(X, T)
+    l2, g2 = net.loss_grad(X, T)
+    assert l1 == l2
+    assert np.array_equal(g1, g2)
+    net.close()
+
+
 def test_gradient_matches_oracle():
     net, ref = _pair(7)
     X, T = _problem(150, 1)

@@ -22,9 +22,10 @@ INCLUDE = os.path.join(ROOT, "include")
 
 SOURCES = ["vefem_fd64.cu", "vefem_gather.cu", "vefem_capi.cu", "vefem_opcount.cpp",
            "vefem_noalloc.cu", "vefem_exact.cu", "vefem_mlp.cu", "vefem_batch.cu",
-           "vefem_stability.cu"]
-# the exact-Jacobian and network kernels are not held to bit-exactness: FMA contraction allowed
-FMAD_ON = {"vefem_exact.cu", "vefem_mlp.cu"}
+           "vefem_stability.cu", "vefem_frontal.cu"]
+# the exact-Jacobian, network and linear-solver kernels are not held to bit-exactness: FMA
+# contraction allowed
+FMAD_ON = {"vefem_exact.cu", "vefem_mlp.cu", "vefem_frontal.cu"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -42,8 +42,9 @@ from the last converged point before the reference's relaxation restart, so
 the continuation follows the branch through folds instead of relaxing across
 them.  The host solves
 with SuperLU in a nested-dissection order (linsolve.py, stand-in for
-MUMPS); the dense lambda row and the arclength column make the matrix
-bordered, and the lambda unknown is ordered last.
+MUMPS) or on the GPU with the panel-frontal LU (frontal.py); the dense lambda
+row and the arclength column make the matrix bordered, and the lambda unknown
+is ordered last.
 """
 from __future__ import annotations
 
@@ -124,18 +125,33 @@ class LambdaRow:
         self.dS = 0.0
 
     def __call__(self, x: np.ndarray, b: np.ndarray, vals):
+        """``vals``: host array, device tensor (FP64) or None."""
         N = self.N
         r0, r1 = self.rowptr[N - 1], self.rowptr[N]
+        slots = self.last_col_slots
+        if vals is not None and not isinstance(vals, np.ndarray):
+            slots = self._device_slots(vals.device)
         if self.mode == "pinned":
             b[N - 1] = x[N - 1] - self.target
             if vals is not None:
-                vals[self.last_col_slots] = 0.0
+                vals[slots] = 0.0
                 vals[r0:r1] = 0.0
                 vals[r1 - 1] = 1.0
         else:
             b[N - 1] = float(np.dot(self.t, x - self.x_o)) - self.dS
-            if vals is not None:
+            if vals is None:
+                pass
+            elif isinstance(vals, np.ndarray):
                 vals[r0:r1] = self.t
+            else:
+                import torch
+                vals[r0:r1] = torch.from_numpy(self.t).to(vals.device)
+
+    def _device_slots(self, device):
+        if getattr(self, "_dslots", None) is None or self._dslots.device != device:
+            import torch
+            self._dslots = torch.from_numpy(self.last_col_slots.astype(np.int64)).to(device)
+        return self._dslots
 
 
 class SecantPredictor:
@@ -164,7 +180,7 @@ class ArclengthContinuation:
 
     def __init__(self, asm, mesh, phys: S.Physics, jacobian: str = "fd64",
                  settings: ArclengthSettings | None = None, outlet_edges: bool = True,
-                 log=None, assembly=None):
+                 log=None, assembly=None, linear_solver="superlu"):
         if phys.nex != 1:
             raise ValueError("arclength continuation needs nex = 1")
         self.asm, self.mesh, self.phys = asm, mesh, phys
@@ -176,7 +192,11 @@ class ArclengthContinuation:
         self.dev = assembly if assembly is not None else \
             NW.DeviceAssembly(asm, rows, values, jacobian, outlet_edges)
         self.lrow = LambdaRow(asm.rowptr, asm.colind)
-        self.solver = LS.SparseLU(asm.rowptr, asm.colind, mesh)
+        # host SuperLU or the GPU frontal LU (linsolve.make_solver); a device
+        # solver takes the AIJ values where the assembly left them
+        self.solver = LS.make_solver(linear_solver, asm.rowptr, asm.colind, mesh)
+        if hasattr(self.dev, "device_values"):
+            self.dev.device_values = LS.on_device(self.solver)
         self.N = asm.N
         self.nn = asm.nnodes
         self.judge_s = 0.0

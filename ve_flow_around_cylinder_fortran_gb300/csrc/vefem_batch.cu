@@ -6,10 +6,15 @@
 // work list of (instance, first element, count) items for the element
 // kernels, which run with a grid of SMs x resident CTAs and walk the work list
 // with a grid stride; the element-batch tile (elements per work item) is
-// chosen per mesh-size class by the autotuner.  The scatter is the single-mesh
-// element-ordered gather per instance, captured as graph nodes (a single
-// scatter over all instances measured slower: each thread had to find its
-// instance and load its tables).
+// chosen per mesh-size class by the autotuner.  The scatter is one persistent
+// launch too: a work list of (instance, kind, first entry, count) items built
+// at create, each item a run of entries of one instance's residual, Jacobian
+// blocks or arclength column, so a CTA reads its instance's tables once per
+// item and no thread searches for its instance.  Every global entry is still
+// the element-ordered sum of the single-mesh gather, bit for bit; with
+// VEFEM_ZERO_FIRST the sums start from zero in place of a memset of b and the
+// AIJ values (the extra items clear the rows the gathers do not own: the
+// lambda row and the lambda entry of b).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -27,6 +32,81 @@ using namespace vefem;
 namespace {
 
 const int EX_TILES[] = {1, 2, 4, 8};         // candidate element-batch tiles of the Jacobian kernel
+
+// scatter work items: a run of entries of one kind of one instance
+enum { SC_RES = 0, SC_JAC = 1, SC_ARC = 2, SC_EXTRA = 3 };
+struct ScatterItem {
+    int inst, kind;
+    int64_t first;
+    int count, pad;
+};
+constexpr int SC_RES_RUN = 2048;     // residual / arclength entries per item
+constexpr int SC_JAC_RUN = 64 * 36;  // Jacobian entries (64 node-pair blocks) per item
+constexpr int SC_THREADS = 256;
+
+// One launch for the scatter of every instance: per item the instance's
+// tables, then the element-ordered sums of the single-mesh gathers
+// (vefem_gather.cu, vefem_exact.cu).  store: start each sum from zero
+// (VEFEM_ZERO_FIRST) instead of the array's value.
+template <class T>
+__global__ void __launch_bounds__(SC_THREADS)
+k_scatter_batched(const BatchInst *__restrict__ insts, const ScatterItem *__restrict__ items,
+                  int nitems, int want_res, int want_jac, int store)
+{
+    for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+        const ScatterItem it = items[w];
+        if ((it.kind == SC_RES && !want_res) || ((it.kind == SC_JAC || it.kind == SC_ARC) && !want_jac) ||
+            (it.kind == SC_EXTRA && !store))
+            continue;
+        const BatchInst &I = insts[it.inst];
+        const GatherArgs g = I.ga;
+        const int64_t end = it.first + it.count;
+        if (it.kind == SC_RES) {
+            const double *rs = I.ea.rs;
+            double *b = I.b;
+            for (int64_t t = it.first + threadIdx.x; t < end; t += SC_THREADS) {
+                const int node = (int)(t / 6), jeq = (int)(t - (int64_t)node * 6);
+                double acc = store ? 0.0 : b[t];
+                const int c0 = g.nptr[node], c1 = g.nptr[node + 1];
+                for (int c = c0; c < c1; c++) acc = acc + rs[(int64_t)g.ncon[c] * 6 + jeq];
+                b[t] = acc;
+            }
+        } else if (it.kind == SC_JAC) {
+            const T *es = static_cast<const T *>(I.es);
+            T *vals = static_cast<T *>(I.vals);
+            for (int64_t t = it.first + threadIdx.x; t < end; t += SC_THREADS) {
+                const int blk = (int)(t / 36);
+                const int r = (int)(t - (int64_t)blk * 36);
+                const int jeq = r / 6, ieq = r - 6 * (r / 6);
+                const int64_t slot = g.rowptr[(int64_t)g.brow[blk] * 6 + jeq] + g.boff[blk] + ieq;
+                T acc = store ? (T)0 : vals[slot];
+                const int c0 = g.bptr[blk], c1 = g.bptr[blk + 1];
+                for (int c = c0; c < c1; c++) acc = acc + es[(int64_t)g.bcon[c] * 36 + r];
+                vals[slot] = acc;
+            }
+        } else if (it.kind == SC_ARC) {
+            const T *as = static_cast<const T *>(I.as);
+            T *vals = static_cast<T *>(I.vals);
+            for (int64_t t = it.first + threadIdx.x; t < end; t += SC_THREADS) {
+                const int node = (int)(t / 6), jeq = (int)(t - (int64_t)node * 6);
+                const int64_t slot = g.rowptr[t + 1] - 1;
+                T acc = store ? (T)0 : vals[slot];
+                const int c0 = g.nptr[node], c1 = g.nptr[node + 1];
+                for (int c = c0; c < c1; c++) acc = acc + as[(int64_t)g.ncon[c] * 6 + jeq];
+                vals[slot] = acc;
+            }
+        } else {
+            // the rows after the node unknowns: the lambda row of the values
+            // (entries first .. end) and the lambda entries of b
+            const int64_t n6 = (int64_t)g.nnodes * 6;
+            if (want_jac) {
+                T *vals = static_cast<T *>(I.vals);
+                for (int64_t t = it.first + threadIdx.x; t < end; t += SC_THREADS) vals[t] = (T)0;
+            }
+            if (want_res && threadIdx.x < g.nex) I.b[n6 + threadIdx.x] = 0.0;
+        }
+    }
+}
 
 int size_class(int nel)
 {
@@ -61,6 +141,8 @@ struct vefem_batch {
     BatchInst *d_inst = nullptr;
     WorkItem *d_res_work = nullptr, *d_ex_work = nullptr;
     int n_res_work = 0, n_ex_work = 0;
+    ScatterItem *d_sc_work = nullptr;
+    int n_sc_work = 0;
     int64_t total_el = 0;
     // scratch
     double *d_rs = nullptr;
@@ -113,6 +195,28 @@ int build_work(vefem_batch *bt)
     BCK(cudaMemcpy(bt->d_ex_work, xw.data(), xw.size() * sizeof(WorkItem), cudaMemcpyHostToDevice));
     bt->n_res_work = (int)rw.size();
     bt->n_ex_work = (int)xw.size();
+    if (!bt->d_sc_work) {
+        std::vector<ScatterItem> sw;
+        for (int i = 0; i < bt->ninst; i++) {
+            const vefem_ctx *c = bt->ctx[i];
+            const int64_t n6 = (int64_t)c->nnodes * 6, nj = (int64_t)c->nblocks * 36;
+            for (int64_t f = 0; f < n6; f += SC_RES_RUN)
+                sw.push_back({i, SC_RES, f, (int)std::min<int64_t>(SC_RES_RUN, n6 - f), 0});
+            for (int64_t f = 0; f < nj; f += SC_JAC_RUN)
+                sw.push_back({i, SC_JAC, f, (int)std::min<int64_t>(SC_JAC_RUN, nj - f), 0});
+            if (c->nex) {
+                for (int64_t f = 0; f < n6; f += SC_RES_RUN)
+                    sw.push_back({i, SC_ARC, f, (int)std::min<int64_t>(SC_RES_RUN, n6 - f), 0});
+                const int64_t r0 = c->h_rowptr[n6], r1 = c->h_rowptr[c->N];
+                for (int64_t f = r0; f < r1; f += SC_RES_RUN)
+                    sw.push_back({i, SC_EXTRA, f, (int)std::min<int64_t>(SC_RES_RUN, r1 - f), 0});
+                if (r1 == r0) sw.push_back({i, SC_EXTRA, r0, 0, 0});
+            }
+        }
+        BCK(cudaMalloc(&bt->d_sc_work, sw.size() * sizeof(ScatterItem)));
+        BCK(cudaMemcpy(bt->d_sc_work, sw.data(), sw.size() * sizeof(ScatterItem), cudaMemcpyHostToDevice));
+        bt->n_sc_work = (int)sw.size();
+    }
     if (bt->graph) {
         cudaGraphExecDestroy(bt->graph);
         bt->graph = nullptr;
@@ -145,13 +249,8 @@ void launch_all(vefem_batch *bt, int flags, bool timing, cudaError_t *err)
     cudaError_t e = cudaSuccess;
     bt->launches = 0;
     if (timing && e == cudaSuccess) e = cudaEventRecord(bt->ev[0], s);
-    if (flags & VEFEM_ZERO_FIRST) {
-        for (int i = 0; i < bt->ninst && e == cudaSuccess; i++) {
-            const BatchInst &I = bt->h_inst[i];
-            if (want_res) e = cudaMemsetAsync(I.b, 0, bt->ctx[i]->N * sizeof(double), s);
-            if (jmode && e == cudaSuccess) e = cudaMemsetAsync(I.vals, 0, bt->ctx[i]->nnz * vsize, s);
-        }
-    }
+    // VEFEM_ZERO_FIRST: the scatter starts its sums from zero (no memsets)
+    const int store = (flags & VEFEM_ZERO_FIRST) ? 1 : 0;
     if (timing && e == cudaSuccess) e = cudaEventRecord(bt->ev[1], s);
     const int res_grid = bt->sms * std::max(1, residual_batched_ctas_per_sm(bt->form, bt->spec));
     const int ex_grid = bt->sms * std::max(1, exact_batched_ctas_per_sm((int)vsize, bt->form, bt->spec));
@@ -179,28 +278,17 @@ void launch_all(vefem_batch *bt, int flags, bool timing, cudaError_t *err)
     }
     if (side && e == cudaSuccess) e = cudaStreamWaitEvent(s, bt->join, 0);
     if (timing && e == cudaSuccess) e = cudaEventRecord(bt->ev[2], s);
-    // scatter: the single-mesh element-ordered gathers, one launch per instance and
-    // array (graph nodes), with each instance's tables as kernel arguments
-    for (int i = 0; i < bt->ninst && e == cudaSuccess; i++) {
-        const BatchInst &I = bt->h_inst[i];
-        if (want_res) {
-            e = launch_gather_residual(I.ga, I.ea.rs, I.b, s);
-            bt->launches++;
-        }
-        if (jmode && e == cudaSuccess) {
-            e = f32 ? launch_gather_jacobian32(I.ga, static_cast<const float *>(I.es),
-                                               static_cast<float *>(I.vals), s)
-                    : launch_gather_jacobian(I.ga, static_cast<const double *>(I.es),
-                                             static_cast<double *>(I.vals), s);
-            bt->launches++;
-            if (bt->nex && e == cudaSuccess) {
-                e = f32 ? launch_gather_arclength32(I.ga, static_cast<const float *>(I.as),
-                                                    static_cast<float *>(I.vals), s)
-                        : launch_gather_arclength(I.ga, static_cast<const double *>(I.as),
-                                                  static_cast<double *>(I.vals), s);
-                bt->launches++;
-            }
-        }
+    // scatter: one persistent launch over the scatter work list
+    if (e == cudaSuccess) {
+        const int grid = std::min(bt->n_sc_work, bt->sms * 8);
+        if (f32)
+            k_scatter_batched<float><<<grid, SC_THREADS, 0, s>>>(bt->d_inst, bt->d_sc_work, bt->n_sc_work,
+                                                                want_res, jmode != 0, store);
+        else
+            k_scatter_batched<double><<<grid, SC_THREADS, 0, s>>>(bt->d_inst, bt->d_sc_work, bt->n_sc_work,
+                                                                 want_res, jmode != 0, store);
+        e = cudaGetLastError();
+        bt->launches++;
     }
     if (timing && e == cudaSuccess) e = cudaEventRecord(bt->ev[3], s);
     *err = e;
@@ -569,7 +657,7 @@ extern "C" int vefem_batch_destroy(vefem_batch *bt)
     if (bt->s) cudaStreamSynchronize(bt->s);
     if (bt->graph) cudaGraphExecDestroy(bt->graph);
     for (vefem_ctx *c : bt->ctx) vefem_destroy(c);
-    void *p[] = {bt->d_inst, bt->d_res_work, bt->d_ex_work,
+    void *p[] = {bt->d_inst, bt->d_res_work, bt->d_ex_work, bt->d_sc_work,
                  bt->d_rs, bt->d_es, bt->d_as};
     for (void *q : p)
         if (q) cudaFree(q);

@@ -120,24 +120,28 @@ __global__ void k_linear_bwd_w(const float *__restrict__ dZ, const float *__rest
     if (o < out && blockIdx.x == 0 && threadIdx.x == 0) gb[o] = accb;
 }
 
-// MSE loss and its gradient: dY = 2 (Y - T) / (n out); loss accumulated in *loss
-__global__ void k_mse(int count, const float *__restrict__ Y, const float *__restrict__ T,
-                      float *__restrict__ dY, float *__restrict__ loss)
+// MSE loss and its gradient: dY = 2 (Y - T) / (n out), *loss = mean (Y - T)^2.
+// One block: each thread sums its strided share in order, then a fixed tree in
+// shared memory -- the same bits on every run (no atomics).
+constexpr int MSE_THREADS = 1024;
+__global__ void __launch_bounds__(MSE_THREADS) k_mse(int count, const float *__restrict__ Y,
+                                                     const float *__restrict__ T,
+                                                     float *__restrict__ dY, float *__restrict__ loss)
 {
-    __shared__ float red[256];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    float d = 0.0f;
-    if (i < count) {
-        d = Y[i] - T[i];
+    __shared__ float red[MSE_THREADS];
+    float acc = 0.0f;
+    for (int i = threadIdx.x; i < count; i += MSE_THREADS) {
+        const float d = Y[i] - T[i];
         dY[i] = 2.0f * d / (float)count;
+        acc += d * d;
     }
-    red[threadIdx.x] = d * d;
+    red[threadIdx.x] = acc;
     __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    for (int s = MSE_THREADS / 2; s > 0; s >>= 1) {
         if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
         __syncthreads();
     }
-    if (threadIdx.x == 0) atomicAdd(loss, red[0] / (float)count);
+    if (threadIdx.x == 0) *loss = red[0] / (float)count;
 }
 
 // Adam on the FP32 masters, then the BF16 copy; t is read from device memory
@@ -270,7 +274,7 @@ void launch_loss(vefem_mlp *m, int n)
 {
     Layer &o = m->L.back();
     const int count = n * o.out;
-    k_mse<<<(count + 255) / 256, 256, 0, m->s>>>(count, o.A, m->T, o.dA, m->loss);
+    k_mse<<<1, MSE_THREADS, 0, m->s>>>(count, o.A, m->T, o.dA, m->loss);
 }
 
 void launch_adam(vefem_mlp *m, float lr)

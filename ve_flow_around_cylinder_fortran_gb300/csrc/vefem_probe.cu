@@ -1,6 +1,7 @@
-// FP64 pipe throughput probe used by the benchmark for the roofline
-// denominator of the FP64 kernels (the measured peaks cover HBM and
-// bf16 only).  Eight independent dependency chains per thread, 8 CTAs per SM.
+// FP64 and FP32 pipe throughput probes used by the benchmark for the roofline
+// denominators of the FP64 kernels and of the FP32 precision-form kernel (the
+// measured peaks cover HBM and bf16 only).  Eight independent
+// dependency chains per thread, 8 CTAs per SM.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -44,6 +45,55 @@ __global__ void k_probe_dmul(double *out, int iters, double a)
 #pragma unroll
     for (int i = 0; i < 8; i++) s += x[i];
     out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+__global__ void k_probe_ffma(float *out, int iters, float a, float b)
+{
+    float x[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) x[i] = threadIdx.x * 1e-3f + i;
+    for (int it = 0; it < iters; it++)
+#pragma unroll
+        for (int i = 0; i < 8; i++) x[i] = fmaf(x[i], a, b);
+    float s = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 8; i++) s += x[i];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+// out[0] FFMA instructions/s (best of 3): the FP32 pipe peak of the
+// precision-form roofline (one FFMA = two operations); returns 0 or a CUDA
+// error code.
+extern "C" int vefem_probe_fp32(int device, double *out)
+{
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return (int)e;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    const int blocks = sms * 8, threads = 256, iters = 16384;
+    float *d = nullptr;
+    if ((e = cudaMalloc(&d, sizeof(float) * blocks * threads)) != cudaSuccess) return (int)e;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    const double ops = 8.0 * iters * (double)blocks * threads;
+    double best = 0.0;
+    for (int rep = 0; rep < 3; rep++) {
+        cudaEventRecord(a);
+        k_probe_ffma<<<blocks, threads>>>(d, iters, 0.9999999f, 1e-7f);
+        cudaEventRecord(b);
+        cudaEventSynchronize(b);
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, a, b);
+        const double r = ops / (ms * 1e-3);
+        if (r > best) best = r;
+    }
+    out[0] = best;
+    e = cudaGetLastError();
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(d);
+    return (int)e;
 }
 
 // out[0] DFMA instructions/s, out[1] DADD/s, out[2] DMUL/s (best of 3 each);

@@ -117,3 +117,34 @@ class SparseLU:
         x = np.empty_like(xp)
         x[self.perm] = xp
         return x
+
+
+def make_solver(kind, rowptr: np.ndarray, colind: np.ndarray, mesh=None, **kw):
+    """The linear solver of the Newton and continuation drivers: ``"superlu"``
+    (host SuperLU in nested-dissection order), ``"frontal"`` (the GPU
+    panel-frontal LU of frontal.py, FP64), ``"auto"`` (frontal for meshes of
+    1,000 elements or more when a GPU is present, else SuperLU), a callable
+    ``kind(rowptr, colind, mesh)`` returning an object with ``factor(vals)``
+    and ``solve(b)``, or such an object itself."""
+    if hasattr(kind, "factor") and hasattr(kind, "solve"):
+        return kind                 # a solver instance, shared between drivers
+    if callable(kind):
+        return kind(rowptr, colind, mesh)
+    if kind == "auto":
+        import torch
+        big = mesh is not None and mesh.nel >= 1000
+        kind = "frontal" if (big and torch.cuda.is_available()) else "superlu"
+    if kind == "superlu":
+        return SparseLU(rowptr, colind, mesh, **kw)
+    if kind == "frontal":
+        if mesh is None:
+            raise ValueError("the frontal solver needs the mesh")
+        from .frontal import FrontalLU
+        return FrontalLU(rowptr, colind, mesh, **kw)
+    raise ValueError(f"unknown linear solver {kind!r}")
+
+
+def on_device(solver) -> bool:
+    """Whether ``solver`` factorises device-resident AIJ values."""
+    return getattr(solver, "device_values", False)
+

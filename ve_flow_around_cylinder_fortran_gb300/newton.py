@@ -170,6 +170,8 @@ class DeviceAssembly:
     def __init__(self, asm: V.BulkAssembler, rows: np.ndarray, values: np.ndarray,
                  jacobian: str = "fd64", outlet_edges: bool = True):
         import torch
+        # True: the AIJ values stay on the device (FP64) for a device solver
+        self.device_values = False
         self.torch = torch
         self.asm = asm
         self.jacobian = jacobian
@@ -204,8 +206,11 @@ class DeviceAssembly:
                                  self.vals if want_jac else None, dflags, on_device=True,
                                  nrows=self.nrows)
         b = self.b.cpu().numpy()
-        vals = self.vals.cpu().numpy().astype(np.float64) if want_jac else None
-        return b, vals
+        if not want_jac:
+            return b, None
+        if self.device_values:
+            return b, self.vals.to(torch.float64)
+        return b, self.vals.cpu().numpy().astype(np.float64)
 
 
 def emergency_solve(newton, TL, EU, log=None, **kw):
@@ -226,12 +231,15 @@ def emergency_solve(newton, TL, EU, log=None, **kw):
 
 
 def natural_continuation(asm, mesh, phys: S.Physics, wis, jacobian: str = "fd64",
-                         tol: float = 1.0e-10, outlet_edges: bool = True, TL=None, log=None):
+                         tol: float = 1.0e-10, outlet_edges: bool = True, TL=None, log=None,
+                         linear_solver="superlu"):
     """Solve at each Weissenberg number of ``wis`` in turn, each from the
     previous solution (the inflow Dirichlet data follow Wi).  Returns the list
     of NewtonResult."""
     out = []
     EU = np.ones(phys.nex)
+    # one solver for all points (the frontal LU's symbolic phase is per mesh)
+    solver = LS.make_solver(linear_solver, asm.rowptr, asm.colind, mesh)
     for wi in wis:
         p = dataclasses.replace(phys, WiN=wi, Wi0=wi)
         asm.set_params(p)
@@ -240,7 +248,7 @@ def natural_continuation(asm, mesh, phys: S.Physics, wis, jacobian: str = "fd64"
             TL, EU = initial_state(mesh, p)
         TL = np.ascontiguousarray(TL)
         nr = NewtonRaphson(DeviceAssembly(asm, rows, values, jacobian, outlet_edges),
-                           asm.rowptr, asm.colind, p.nex, mesh)
+                           asm.rowptr, asm.colind, p.nex, mesh, linear_solver=solver)
         res = emergency_solve(nr, TL, EU, log=log, tol=tol)
         if not res.converged:
             raise RuntimeError(f"Newton did not converge at Wi = {wi}")
@@ -253,14 +261,18 @@ class NewtonRaphson:
     """loopNewtonRaphson for one parameter point.  ``assembly(TL, EU, want_jac)``
     returns the host residual and AIJ values with the Dirichlet rows applied."""
 
-    def __init__(self, assembly, rowptr: np.ndarray, colind: np.ndarray, nex: int, mesh=None):
+    def __init__(self, assembly, rowptr: np.ndarray, colind: np.ndarray, nex: int, mesh=None,
+                 linear_solver="superlu"):
         self.assembly = assembly
         self.rowptr = rowptr
         self.colind = colind
         self.nex = nex
         self.N = len(rowptr) - 1
-        # nested-dissection order from the mesh when given, else column AMD
-        self.solver = LS.SparseLU(rowptr, colind, mesh)
+        # host SuperLU (nested-dissection order from the mesh when given, else
+        # column AMD) or the GPU frontal LU (linsolve.make_solver)
+        self.solver = LS.make_solver(linear_solver, rowptr, colind, mesh)
+        if hasattr(assembly, "device_values"):
+            assembly.device_values = LS.on_device(self.solver)
 
     def solve(self, TL: np.ndarray, EU: np.ndarray, tol: float = 1.0e-8,
               res_tol: float | None = None, max_iter: int = NITER, mnr: bool = True,

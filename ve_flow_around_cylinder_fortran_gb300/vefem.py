@@ -39,7 +39,10 @@ EXPORTED = ["vefem_abi_version", "vefem_create", "vefem_set_params", "vefem_asse
             "vefem_batch_create", "vefem_batch_set_params", "vefem_assemble_batched",
             "vefem_batch_autotune", "vefem_batch_set_tiles", "vefem_batch_info",
             "vefem_batch_last_timing", "vefem_batch_destroy", "vefem_batch_last_error",
-            "vefem_stability_pattern", "vefem_stability_assemble"]
+            "vefem_stability_pattern", "vefem_stability_assemble",
+            "vefem_frontal_create", "vefem_frontal_factor", "vefem_frontal_solve",
+            "vefem_frontal_destroy", "vefem_frontal_last_error"]
+VEFEM_ERR_SINGULAR = 6
 BATCH_CLASSES = 6
 
 
@@ -114,6 +117,13 @@ def load(path: str = LIB_PATH):
     L.vefem_batch_last_error.restype = ctypes.c_char_p
     L.vefem_stability_pattern.argtypes = [P, P, P, P, P]
     L.vefem_stability_assemble.argtypes = [P, P, I, P, I, P, P, I]
+    L.vefem_frontal_create.argtypes = [I, I, P, P, P, P, P, P, P, I64, ctypes.POINTER(P)]
+    L.vefem_frontal_factor.argtypes = [P, P, P, ctypes.c_double, P]
+    L.vefem_frontal_solve.argtypes = [P, P, P, P, P]
+    L.vefem_frontal_destroy.argtypes = [P]
+    L.vefem_frontal_destroy.restype = None
+    L.vefem_frontal_last_error.argtypes = [P]
+    L.vefem_frontal_last_error.restype = ctypes.c_char_p
     _lib = L
     return L
 
