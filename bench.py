@@ -19,11 +19,17 @@ unknown (Nex = 1).  Synthetic seeded state (no dataset exists for this path).
 * cpu_baseline: the CPU oracle (a C restatement of the reference algorithm)
   on all host cores, on a bounded sample of the same workload;
 * continuation: the metric's continuation comparison, Wi 0.1 -> 1.0 by
-  pseudo-arclength on a smaller mesh (``--cont-nel``, 500 quads by default so
-  the run stays within minutes): the plain FP64 path (FD64 Jacobian, tangent
-  predictor) against the learned + mixed path (FP32 Jacobian, learned
-  predictor), wall time, steps/s, Newton iterations and LU factorisations.
-  ``--continuation-only --cont-nel N`` runs only this comparison;
+  pseudo-arclength on the 20,000-quad mesh (``--cont-nel``): the plain FP64
+  path (FD64 Jacobian, tangent predictor, the reference's factorisation reuse)
+  against the learned + mixed path (FP32 Jacobian, learned predictor,
+  contraction-monitored reuse), both with the GPU frontal LU; wall time,
+  steps/s, Newton iterations, factorisations and the wall-time ratio.
+  ``--ablations`` and ``--secant`` add arms; ``--continuation-only`` runs
+  only this comparison;
+* newton_precision: the precision form's Newton solves on 40,000 quads
+  (Giesekus, SQRT; ``--newton-nel``): FP64 forward-difference Jacobian
+  against FP32 exact Jacobian + FP64 residual, iterations, factorisations and
+  the converged solution's error against the FP64 one, every run;
 * batched: the batched form, 64 instances of 2,000-20,000 quads at Wi in
   [0.1, 1.0], one persistent launch per kernel replayed as a CUDA graph,
   against one call per instance;
@@ -73,15 +79,16 @@ def parse_args():
     ap.add_argument("--impl", choices=["vefem", "reference"], default="vefem")
     ap.add_argument("--nel", type=int, default=40000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cont-nel", type=int, default=500,
+    ap.add_argument("--cont-nel", type=int, default=20000,
                     help="mesh of the continuation comparison (0 = skip it)")
     ap.add_argument("--cont-wi", type=float, default=1.0, help="Wi the continuation ends at")
     ap.add_argument("--cont-log", action="store_true",
                     help="with --continuation-only: every Newton iteration and step on stderr")
-    ap.add_argument("--no-secant", action="store_true",
-                    help="leave out the secant-predictor arm of the continuation comparison")
-    ap.add_argument("--no-ablations", action="store_true",
-                    help="leave out the ablation arms of the continuation comparison")
+    ap.add_argument("--secant", action="store_true",
+                    help="add the secant-predictor arm to the continuation comparison")
+    ap.add_argument("--ablations", action="store_true",
+                    help="add the ablation arms to the continuation comparison (the learned arm "
+                         "with the reference's reuse rules; POD extrapolation without the network)")
     ap.add_argument("--cont-arms", default="",
                     help="comma-separated arm names of the continuation comparison to run "
                          "(default: all)")
@@ -663,8 +670,8 @@ def run_vefem(args):
     if args.continuation_only:
         if rank == 0:
             out = continuation_compare(
-                args.cont_nel, args.cont_wi, dev, secant=not args.no_secant,
-                ablations=not args.no_ablations,
+                args.cont_nel, args.cont_wi, dev, secant=args.secant,
+                ablations=args.ablations,
                 only=[a for a in args.cont_arms.split(",") if a] or None,
                 linear_solver=args.linear_solver,
                 step_log=(lambda m: print(m, file=sys.stderr, flush=True)) if args.cont_log else None)
@@ -834,18 +841,37 @@ def run_vefem(args):
     }
     line.update(forms)
     asm.close()
+    def leg(name, fn):
+        # a secondary measurement that fails is reported in the line, not fatal
+        try:
+            line[name] = fn()
+        except Exception as exc:      # noqa: BLE001
+            import traceback
+            traceback.print_exc()
+            line[name] = {"error": f"{type(exc).__name__}: {exc}"}
+
     if world == 1 and args.batch_inst > 0:
-        line["batched"] = batched_compare(args.batch_inst, max(3, args.steps // 2), args.warmup, dev)
+        leg("batched", lambda: batched_compare(args.batch_inst, max(3, args.steps // 2),
+                                               args.warmup, dev))
     if world == 1 and args.newton_nel > 0:
-        line["newton_precision"] = newton_precision_compare(args.newton_nel, dev,
-                                                            linear_solver=args.linear_solver)
+        leg("newton_precision", lambda: newton_precision_compare(
+            args.newton_nel, dev, linear_solver=args.linear_solver))
+        npr = line["newton_precision"]
+        if "fp32_jacobian" in npr:
+            line["fp32_jacobian"]["newton"] = {
+                "workload": npr["workload"],
+                "iterations": [x["iterations"] for x in npr["fp32_jacobian"]["solves"]],
+                "factorisations": [x["factorisations"] for x in npr["fp32_jacobian"]["solves"]],
+                "fp64_iterations": [x["iterations"] for x in npr["fd64"]["solves"]],
+                "solution_rel_err_2norm": npr["solution_rel_err_2norm"],
+                "solution_rel_err_maxnorm": npr["solution_rel_err_maxnorm"]}
     if world == 1 and args.cont_nel > 0:
-        line["continuation"] = continuation_compare(args.cont_nel, args.cont_wi, dev,
-                                                    secant=not args.no_secant,
-                                                    ablations=not args.no_ablations)
+        leg("continuation", lambda: continuation_compare(
+            args.cont_nel, args.cont_wi, dev, secant=args.secant, ablations=args.ablations,
+            linear_solver=args.linear_solver))
     if world == 1 and args.stab_nel > 0:
-        line["stability"] = stability_compare(args.stab_nel, max(3, args.steps // 4), args.warmup,
-                                              dev, cpu=not args.no_cpu_baseline)
+        leg("stability", lambda: stability_compare(args.stab_nel, max(3, args.steps // 4),
+                                                   args.warmup, dev, cpu=not args.no_cpu_baseline))
     # the CPU baseline runs last: its OpenMP worker threads stay on the host
     # cores afterwards and would slow the host side of the parts above
     if world == 1 and not args.no_cpu_baseline:

@@ -189,7 +189,7 @@ def stability_elements(phys, conn, xyz, TLb, TLd, KwN: float, kz: bool = True, j
                                _p(xyz), _p(TLb), _p(TLd), e0, e1, _p(ra), _p(rb), _p(A), _p(B),
                                nthreads)
     if rc:
-        raise ValueError(f"ora_stability_batch: {rc} (T form and non-FENE models only)")
+        raise ValueError(f"ora_stability_batch: {rc} (T form only)")
     return ra, rb, A, B
 
 

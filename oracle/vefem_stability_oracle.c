@@ -121,7 +121,30 @@ static void extra_flow_unknowns_stab(gp_t *g, double KwN)
     for (int i = 0; i < 3; i++) g->G2U[N][i] = -(KwN * KwN) * g->U_f[i];
 }
 
-/* conEQ_*_Stability (Constitutive_Models_Stability_mod.F90:96-225) */
+/* setFENEMaterialDerivativeStability (Constitutive_Models_Stability_mod.F90:294-328):
+ * the perturbation of U . grad f_T, with grad f_T from the trace of grad T */
+static double fene_md_stab(const prm_t *p, double WiN, const gp_t *b, const gp_t *d)
+{
+    double dfb[3] = {0.0, 0.0, 0.0}, dfd[3] = {0.0, 0.0, 0.0};
+    for (int i = 0; i < 3; i++)
+        for (int c = 0; c < 3; c++) {
+            dfb[c] = dfb[c] + b->dTdXi[i][i][c];
+            dfd[c] = dfd[c] + d->dTdXi[i][i][c];
+        }
+    const double den = (p->model == M_FENE_P) ? p->VeN : (p->VeN - (double)NDIM);
+    for (int c = 0; c < 3; c++) {
+        dfb[c] = (WiN / (1.0 - p->BvN)) * dfb[c] / den;
+        dfd[c] = (WiN / (1.0 - p->BvN)) * dfd[c] / den;
+    }
+    double MD = 0.0;
+    for (int i = 0; i < 3; i++) {
+        const double term = ((b->f_T) * dfd[i] - (d->f_T) * dfb[i]) / (b->f_T);
+        MD = MD + (d->U_f[i]) * dfb[i] + (b->U_f[i]) * term;
+    }
+    return MD;
+}
+
+/* conEQ_*_Stability (Constitutive_Models_Stability_mod.F90:96-289) */
 static int con_eq_T_stab(const prm_t *p, double WiN, const gp_t *b, gp_t *d)
 {
     double trT_d = trace3(d->S);
@@ -152,13 +175,48 @@ static int con_eq_T_stab(const prm_t *p, double WiN, const gp_t *b, gp_t *d)
         d->f[0] = 0.0; d->f[1] = 0.0; d->f[2] = 0.0;
         d->g[0] = 0.0; d->g[1] = 0.0;
         return 0;
+    case M_FENE_CR: {   /* :236-260, N = Ndim of the base problem */
+        d->f_T = (WiN * trT_d / (1.0 - BvN)) / (p->VeN - (double)NDIM);
+        d->f[0] = d->f_T;
+        const double MD = fene_md_stab(p, WiN, b, d);
+        d->f[1] = d->f_T - WiN * MD / (b->f_T);
+        d->f[2] = 0.0;
+        d->g[0] = d->f_T; d->g[1] = d->g[0];
+        return 0;
+    }
+    case M_FENE_P: {    /* :264-289 */
+        d->f_T = (WiN * trT_d / (1.0 - BvN)) / p->VeN;
+        d->f[0] = 0.0;
+        const double MD = fene_md_stab(p, WiN, b, d);
+        d->f[1] = d->f_T - WiN * MD / (b->f_T);
+        d->f[2] = 0.0;
+        d->g[0] = 0.0; d->g[1] = d->f_T;
+        return 0;
+    }
     default:
-        return -1;   /* FENE models: not restated */
+        return -1;
     }
 }
 
-/* strongFormConEQ_Stability :55-94 with setUCDStability :310-331 and
- * setStressTensorStability :335-351 (T form, no FENE terms) */
+/* Con_EQ_time of the perturbation (strongFormConEQ_Stability :85-93) */
+static void con_eq_time_stab(const prm_t *p, double WiN, const gp_t *b, const gp_t *d,
+                             double ceqt[3][3])
+{
+    double term_I = 0.0;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) ceqt[i][j] = WiN * (d->S[i][j]);
+    if (p->model == M_FENE_CR || p->model == M_FENE_P) {
+        if (p->model == M_FENE_P) term_I = -(1.0 - p->BvN) * (d->f_T) / (b->f_T);
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++)
+                ceqt[i][j] = ceqt[i][j] - WiN * (d->f_T) * b->S[i][j] / (b->f_T);
+    }
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) ceqt[i][j] = ceqt[i][j] + term_I * I3[i][j];
+}
+
+/* strongFormConEQ_Stability :55-94 with setUCDStability :330-351 and
+ * setStressTensorStability :355-371 (T form) */
 static void strong_form_con_eq_T_stab(const prm_t *p, double WiN, const gp_t *b, gp_t *d)
 {
     for (int i = 0; i < 3; i++)
@@ -192,6 +250,9 @@ static void strong_form_con_eq_T_stab(const prm_t *p, double WiN, const gp_t *b,
     matmul3(d->S, b->GU, M4);
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++) UCD[i][j] = UCD[i][j] - M1[i][j] - M2[i][j] - M3[i][j] - M4[i][j];
+    /* term_I of FENE-P */
+    double term_I = 0.0;
+    if (p->model == M_FENE_P) term_I = fene_md_stab(p, WiN, b, d) / (b->f_T);
     /* term_T */
     double SbSd[3][3], SdSb[3][3], SbSb[3][3];
     matmul3(b->S, d->S, SbSd);
@@ -202,7 +263,7 @@ static void strong_form_con_eq_T_stab(const prm_t *p, double WiN, const gp_t *b,
             double term_T = (b->f[2]) * (SbSd[i][j] + SdSb[i][j]) + (d->f[2]) * SbSb[i][j]
                             + (d->f[1]) * b->S[i][j] + (b->f[1]) * d->S[i][j];
             double term_G = (b->f[0]) * (d->G_dot[i][j]) + (d->f[0]) * (b->G_dot[i][j]);
-            d->Con_EQ[i][j] = WiN * UCD[i][j] + term_T - (1.0 - p->BvN) * (term_G + 0.0 * I3[i][j]);
+            d->Con_EQ[i][j] = WiN * UCD[i][j] + term_T - (1.0 - p->BvN) * (term_G + term_I * I3[i][j]);
         }
 }
 
@@ -263,9 +324,8 @@ static void residual_bulk_stab(const prm_t *p, double WiN, double KwN, int kz, c
         double mt[3];
         strong_form_momentum_stab(p, &gb, &gd, mt);
         gd.Continuity = trace3(gd.GU);     /* strongFormContinuity */
-        double ceqt[3][3];                 /* Con_EQ_time (T form, no FENE) */
-        for (int i = 0; i < 3; i++)
-            for (int j = 0; j < 3; j++) ceqt[i][j] = WiN * (gd.S[i][j]);
+        double ceqt[3][3];                 /* Con_EQ_time */
+        con_eq_time_stab(p, WiN, &gb, &gd, ceqt);
         gd.mag_con_EQ = ddot3(gb.Con_EQ, gd.Con_EQ);
         gd.mag_con_EQ = gd.mag_con_EQ / (2.0 * gb.mag_con_EQ + 1.0e-12);
         /* the steady base has Con_EQ_time = 0, so mag_con_EQ_time of the
@@ -372,7 +432,7 @@ int ora_stability_batch(const int *ip, const double *dp, double KwN, int kz, int
     prm_t p;
     unpack_params(ip, dp, &p);
     if (p.form != FORM_T) return -2;
-    if (p.model == M_FENE_CR || p.model == M_FENE_P) return -3;
+
     gauss_t G;
     gauss_tables(&G);
 #ifdef _OPENMP

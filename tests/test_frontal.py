@@ -38,9 +38,24 @@ def test_frontal_matches_scipy(nex, panel):
     assert np.linalg.norm(A @ lu.solve(b2) - b2) <= lu.check_tol * np.linalg.norm(b2)
 
 
-def test_symbolic_phase_invariants():
+@pytest.mark.parametrize("nex", [0, 1])
+def test_delayed_pressures_match_scipy(nex):
+    """The fallback ordering (every pressure eliminated with the last panel
+    that touches one of its element-mates) solves the same system."""
+    mesh, rp, ci, v, b, A = _bordered(200, nex)
+    x_ref = spla.spsolve(A.tocsc(), b)
+    plain = FR.FrontalLU(rp, ci, mesh, panel=5, device="cpu")
+    lu = FR.FrontalLU(rp, ci, mesh, panel=5, device="cpu", delay_pressure=True).factor(v)
+    assert lu.f_sz.mean() > plain.f_sz.mean()          # the pressures stay in the fronts longer
+    x = lu.solve(b)
+    assert np.linalg.norm(x - x_ref) <= 1e-9 * np.linalg.norm(x_ref)
+    assert np.linalg.norm(A @ x - b) <= 1e-12 * np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("delay", [False, True])
+def test_symbolic_phase_invariants(delay):
     mesh, rp, ci, v, b, A = _bordered(120, 1)
-    lu = FR.FrontalLU(rp, ci, mesh, panel=4, device="cpu")
+    lu = FR.FrontalLU(rp, ci, mesh, panel=4, device="cpu", delay_pressure=delay)
     N = len(rp) - 1
     piv = np.concatenate([p.numpy() for p in lu.idxP])
     # every unknown is eliminated exactly once; the border with the last panel

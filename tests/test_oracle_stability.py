@@ -15,12 +15,15 @@ from ve_flow_around_cylinder_fortran_gb300 import mesh as M
 from ve_flow_around_cylinder_fortran_gb300 import state as S
 
 
-def _case(model="oldroyd_b", seed=1):
+def _case(model="oldroyd_b", seed=1, L2=40.0):
     mesh = M.build_cylinder_mesh(60, exact=False)
     if model == "oldroyd_b":
         phys = S.oldroyd_b(0.5, 0.59, "T", nex=0)
-    else:
+    elif model == "giesekus":
         phys = S.giesekus(0.2, 0.5, 0.59, "T", nex=0)
+    else:
+        phys = S.Physics(model={"fene_cr": "FENE-CR", "fene_p": "FENE-P"}[model], form="T",
+                         WiN=0.5, Wi0=0.5, BvN=0.59, VeN=L2, nex=0)
     TL, _ = S.seeded_state(mesh.xyz, phys, seed=seed)
     nn = mesh.nnodes
     TLb = np.zeros((10, nn))
@@ -29,7 +32,7 @@ def _case(model="oldroyd_b", seed=1):
     return mesh, phys, TLb
 
 
-@pytest.mark.parametrize("model", ["oldroyd_b", "giesekus"])
+@pytest.mark.parametrize("model", ["oldroyd_b", "giesekus", "fene_cr", "fene_p"])
 def test_linear_in_the_perturbation(model):
     mesh, phys, TLb = _case(model)
     rng = np.random.default_rng(0)
@@ -42,8 +45,9 @@ def test_linear_in_the_perturbation(model):
         assert np.max(np.abs(r[3][q])) == 0.0
 
 
-def test_fd_blocks_are_the_operator():
-    mesh, phys, TLb = _case()
+@pytest.mark.parametrize("model", ["oldroyd_b", "fene_cr", "fene_p"])
+def test_fd_blocks_are_the_operator(model):
+    mesh, phys, TLb = _case(model)
     _, _, A, B = O.stability_elements(phys, mesh.conn, mesh.xyz, TLb, np.zeros((10, mesh.nnodes)),
                                       1.5)
     x = np.random.default_rng(1).standard_normal((10, mesh.nnodes))
@@ -84,7 +88,25 @@ def test_spanwise_velocity_decouples_at_k0():
         assert np.max(np.abs(M_[:, :, inn][:, :, :, :, out])) == 0.0
 
 
-def test_fene_and_sqrt_are_rejected():
+@pytest.mark.parametrize("model", ["fene_cr", "fene_p"])
+def test_fene_tends_to_oldroyd_b(model):
+    """FENE-CR and FENE-P with extensibility L^2 -> infinity are Oldroyd-B
+    (f_T -> 1, its material derivative -> 0): their stability blocks approach
+    the Oldroyd-B ones; at L^2 = 40 they differ."""
+    mesh, ob, TLb = _case("oldroyd_b")
+    _, _, Ao, Bo = O.stability_elements(ob, mesh.conn, mesh.xyz, TLb, np.zeros_like(TLb), 1.5)
+    for L2, close in ((1e12, True), (40.0, False)):
+        _, fene, _ = _case(model, L2=L2)
+        _, _, Af, Bf = O.stability_elements(fene, mesh.conn, mesh.xyz, TLb, np.zeros_like(TLb), 1.5)
+        dA = np.max(np.abs(Af - Ao)) / np.max(np.abs(Ao))
+        dB = np.max(np.abs(Bf - Bo)) / np.max(np.abs(Bo))
+        if close:
+            assert dA < 1e-8 and dB < 1e-8
+        else:
+            assert dA > 1e-4
+
+
+def test_sqrt_is_rejected():
     mesh, phys, TLb = _case()
     import dataclasses
     with pytest.raises(ValueError):

@@ -30,7 +30,8 @@
 // Solve (two launches per panel, replayed from a CUDA graph): forward
 // y_P = A^-1 b_P, b_F += (-C A^-1) b_P; backward x_P = y_P - (A^-1 B) x_F.  Sums
 // run in a fixed order (warp-strided, then a fixed shuffle tree): results are
-// reproducible run to run.
+// reproducible run to run.  (One launch of one 16-CTA cluster with cluster
+// barriers between panels measured slower: the FP64 rate of 16 SMs bounds it.)
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -45,7 +46,6 @@
 namespace {
 
 constexpr int NB = 16;   // pivots per Gauss-Jordan step
-constexpr int TILE = 32; // output tile of the update kernel (TILE x TILE)
 
 // Positive doubles order like their bit patterns: atomicMin on the bits.
 __device__ void atomic_min_pos(unsigned long long *addr, double v)
@@ -57,8 +57,8 @@ __device__ void atomic_min_pos(unsigned long long *addr, double v)
 // the reciprocal, r <- r + r (1 - x r) (quadratic convergence: ~2^-23 ->
 // ~2^-46 -> rounding level).  A handful of FP64 instructions instead of a full
 // IEEE division, which matters on the critical path of the pivot-block
-// inversion (FP64 instructions issue at 2 lanes per clock per SM on this GPU).
-// Values outside the single-precision range take the IEEE division.
+// inversion (a warp issues an FP64 instruction every few tens of clocks on this
+// GPU).  Values outside the single-precision range take the IEEE division.
 __device__ __forceinline__ double recip(double x)
 {
     const float xf = (float)x;
@@ -71,151 +71,274 @@ __device__ __forceinline__ double recip(double x)
     return fma(r, e, r);
 }
 
-// D^-1 of the kb x kb block at M[k0][k0] (leading dimension n) by Gauss-Jordan
-// without pivoting, in one warp: lane c owns column c of [D | I] (D padded to
-// NB x NB with the identity), kept in shared memory column-major (padded
-// stride: no bank conflicts).  The pivot loop is not unrolled (compact code:
-// it runs once per launch, so a long unrolled body would mostly wait for
-// instruction fetches).  The inverse lands in inv[NB][NB] (shared, row-major).
-// A pivot at most tol times the largest |entry| of the block (or not finite)
-// sets *err; the smallest |pivot| / largest |entry| goes to *minpiv.
-__device__ void warp_invert(const double *__restrict__ M, int64_t n, int k0, int kb, double tol,
-                            double (*A)[NB + 1], double (*inv)[NB], int *err,
-                            unsigned long long *minpiv, bool report)
+// In-place Gauss-Jordan inversion without pivoting of the NB x NB block held
+// in A (shared, column-major: A[column][row]; columns 0..NB-1 the block padded
+// with the identity, columns NB..2NB-1 the identity on entry and the inverse on
+// exit), by threads 0..127 of the block (named barrier 1), so that other warps
+// of the block can work meanwhile: thread = (column, quarter of the rows), the
+// FP64 work of a pivot step spread over four warps.  Returns (to the 128
+// threads) the smallest |pivot| over the largest |entry| of the kb x kb block,
+// or -1 when a pivot is at most tol times that largest entry or not finite.
+__device__ __forceinline__ void bar128() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+
+__device__ double block_invert(double (*A)[NB + 1], int kb, double tol, double *s_red)
 {
-    const int c = threadIdx.x & 31;
+    const int t = threadIdx.x;
+    const int c = t & 31, q = (t >> 5) & 3;
     double amax = 0.0;
+    if (c < kb) {
 #pragma unroll
-    for (int r = 0; r < NB; r++) {
-        double v;
-        if (c < NB)
-            v = (r < kb && c < kb) ? M[(int64_t)(k0 + r) * n + k0 + c] : (r == c ? 1.0 : 0.0);
-        else
-            v = (r == c - NB) ? 1.0 : 0.0;
-        A[c][r] = v;
-        if (c < kb && r < kb) amax = fmax(amax, fabs(v));
+        for (int u = 0; u < 4; u++)
+            if (q * 4 + u < kb) amax = fmax(amax, fabs(A[c][q * 4 + u]));
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
-    __syncwarp();
+    if (c == 0) s_red[q] = amax;
+    bar128();
+    amax = fmax(fmax(s_red[0], s_red[1]), fmax(s_red[2], s_red[3]));
     bool bad = !(amax > 0.0) || !isfinite(amax);
     const double floor_ = tol * amax;
     double pmin = INFINITY;
 #pragma unroll 1
     for (int p = 0; p < NB; p++) {
-        double f[NB];
-#pragma unroll
-        for (int r = 0; r < NB; r++) f[r] = A[p][r];      // column p (broadcast reads)
         const double piv = A[p][p];
         if (p < kb) {
-            const double ap = fabs(piv);
-            pmin = fmin(pmin, ap);
-            if (!(ap > floor_) || !isfinite(piv)) bad = true;
+            pmin = fmin(pmin, fabs(piv));
+            if (!(fabs(piv) > floor_) || !isfinite(piv)) bad = true;
         }
         const double rp = A[c][p] * recip(piv);
-        __syncwarp();
+        double f[4];
 #pragma unroll
-        for (int r = 0; r < NB; r++) A[c][r] = (r == p) ? rp : fma(-f[r], rp, A[c][r]);
-        __syncwarp();
-    }
-    if (c >= NB) {
+        for (int u = 0; u < 4; u++) f[u] = A[p][q * 4 + u];
+        bar128();
 #pragma unroll
-        for (int r = 0; r < NB; r++) inv[r][c - NB] = A[c][r];
+        for (int u = 0; u < 4; u++) {
+            const int r = q * 4 + u;
+            A[c][r] = (r == p) ? rp : fma(-f[u], rp, A[c][r]);
+        }
+        bar128();
     }
-    if (report && c == 0) {
-        if (bad) atomicExch(err, 1);
-        const double rel = pmin / amax;
-        if (rel < INFINITY && isfinite(rel)) atomic_min_pos(minpiv, rel);
-    }
+    return bad ? -1.0 : pmin / amax;
 }
 
-// Step part 1: D^-1 (every CTA, one warp), T = D^-1 M[K,:] for the CTA's 16
-// columns (written to Tbuf and into the pivot rows of M, pivot columns left
-// for part 2), and the copy C = M[:,K] of the CTA's 16 rows.
-__global__ void __launch_bounds__(128) k_gj_prep(double *__restrict__ M, int n, int k0, int kb,
-                                                 double *__restrict__ Tbuf, double *__restrict__ Cbuf,
-                                                 double *__restrict__ invbuf, int *err,
-                                                 unsigned long long *minpiv, double tol)
+// First step of a panel: D^-1 of the first pivot block (every CTA) and
+// T = D^-1 M[K,:] for the CTA's 32 columns.  128 threads.
+__global__ void __launch_bounds__(128) k_gj_start(const double *__restrict__ M, int n, int kb,
+                                                  double *__restrict__ Tbuf, double *__restrict__ invbuf,
+                                                  int *err, unsigned long long *minpiv, double tol)
 {
-    __shared__ double sA[32][NB + 1];
-    __shared__ double sInv[NB][NB];
+    __shared__ double sA[2 * NB][NB + 1];
+    __shared__ double s_red[4];
     const int t = threadIdx.x;
-    if (t < 32) warp_invert(M, n, k0, kb, tol, sA, sInv, err, minpiv, blockIdx.x == 0);
+    for (int u = t; u < 2 * NB * NB; u += blockDim.x) {
+        const int c = u / NB, r = u % NB;
+        double v;
+        if (c < NB)
+            v = (r < kb && c < kb) ? M[(int64_t)r * n + c] : (r == c ? 1.0 : 0.0);
+        else
+            v = (r == c - NB) ? 1.0 : 0.0;
+        sA[c][r] = v;
+    }
     __syncthreads();
-    // the inverse for the update kernel (padded rows/columns are the identity's)
-    if (blockIdx.x == 0)
-        for (int u = t; u < NB * NB; u += blockDim.x) invbuf[u] = sInv[u / NB][u % NB];
-    // T for columns j0..j0+15: thread = (column, pair of pivot rows)
-    const int j = blockIdx.x * 16 + (t & 15);
-    const int g = t >> 4;
-    if (j < n && (j < k0 || j >= k0 + kb)) {
+    const double rel = block_invert(sA, kb, tol, s_red);
+    if (blockIdx.x == 0) {
+        for (int u = t; u < NB * NB; u += blockDim.x) invbuf[u] = sA[NB + u % NB][u / NB];
+        if (t == 0) {
+            if (rel < 0.0) atomicExch(err, 1);
+            else atomic_min_pos(minpiv, rel);
+        }
+    }
+    const int j = blockIdx.x * 32 + (t & 31);
+    const int g = t >> 5;
+    if (j < n) {
         double m[NB];
 #pragma unroll
-        for (int l = 0; l < NB; l++) m[l] = l < kb ? M[(int64_t)(k0 + l) * n + j] : 0.0;
+        for (int l = 0; l < NB; l++) m[l] = l < kb ? M[(int64_t)l * n + j] : 0.0;
 #pragma unroll
-        for (int kk = 0; kk < 2; kk++) {
-            const int k = g * 2 + kk;
-            double s = 0.0;
+        for (int kk = 0; kk < 4; kk++) {
+            const int k = g * 4 + kk;
+            double acc = 0.0;
 #pragma unroll
-            for (int l = 0; l < NB; l++) s = fma(sInv[k][l], m[l], s);
-            Tbuf[(int64_t)k * n + j] = s;
-            if (k < kb) M[(int64_t)(k0 + k) * n + j] = s;
+            for (int l = 0; l < NB; l++) acc = fma(sA[NB + l][k], m[l], acc);
+            Tbuf[(int64_t)k * n + j] = acc;
         }
-    }
-    // C = M[i, K] for rows i0..i0+15
-    for (int u = t; u < 16 * NB; u += blockDim.x) {
-        const int i = blockIdx.x * 16 + u / NB, l = u % NB;
-        if (i < n) Cbuf[(int64_t)i * NB + l] = l < kb ? M[(int64_t)i * n + k0 + l] : 0.0;
     }
 }
 
-// Step part 2: every entry outside the pivot rows (and the pivot block itself).
-__global__ void __launch_bounds__(256) k_gj_update(double *__restrict__ M, int n, int k0, int kb,
-                                                   const double *__restrict__ Tbuf,
-                                                   const double *__restrict__ Cbuf,
-                                                   const double *__restrict__ invbuf)
+// The new value of entry (i, j) in a Gauss-Jordan step on pivots
+// K = [k0, k0+kb): C the row's K entries (Min[i, K]), T = D^-1 Min[K,:],
+// inv = D^-1.  One function for every caller, so that the look-ahead's
+// recomputed pivot block equals the written entries bit for bit.
+__device__ __forceinline__ double gj_entry(const double *__restrict__ Min, int n, int i, int j, int k0,
+                                           int kb, const double *ci, const double (*sT)[32], int cc,
+                                           const double (*sInv)[NB])
 {
-    __shared__ double sC[TILE][NB + 1];
-    __shared__ double sT[NB][TILE];
-    __shared__ double sInv[NB][NB];
-    const int t = threadIdx.x;
-    const int i0 = blockIdx.y * TILE, j0 = blockIdx.x * TILE;
-    for (int u = t; u < TILE * NB; u += blockDim.x) {
-        const int r = u / NB, l = u % NB;
-        sC[r][l] = (i0 + r < n) ? Cbuf[(int64_t)(i0 + r) * NB + l] : 0.0;
-        const int k = u / TILE, c = u % TILE;
-        sT[k][c] = (j0 + c < n) ? Tbuf[(int64_t)k * n + j0 + c] : 0.0;
+    const bool iK = i >= k0 && i < k0 + kb, jK = j >= k0 && j < k0 + kb;
+    if (iK) return jK ? sInv[i - k0][j - k0] : sT[i - k0][cc];
+    double acc = 0.0;
+    if (jK) {
+#pragma unroll
+        for (int l = 0; l < NB; l++) acc = fma(ci[l], sInv[l][j - k0], acc);
+        return -acc;
     }
-    if (t < NB * NB) sInv[t / NB][t % NB] = invbuf[t];
-    __syncthreads();
-    const int r = t >> 3;            // tile row
-    const int c0 = (t & 7) * 4;      // 4 consecutive tile columns
-    const int i = i0 + r;
-    if (i >= n) return;
-    const bool iK = i >= k0 && i < k0 + kb;
-    double ci[NB];
 #pragma unroll
-    for (int l = 0; l < NB; l++) ci[l] = sC[r][l];
+    for (int l = 0; l < NB; l++) acc = fma(ci[l], sT[l][cc], acc);
+    return Min[(int64_t)i * n + j] - acc;
+}
+
+// One Gauss-Jordan step on pivots K = [k0, k0+kb): reads Min (the matrix
+// before the step), writes every entry of Mout; T = D^-1 Min[K,:] and D^-1
+// come from the previous launch (Tcur, invcur).
+//
+// Blocks 0 .. nlook-1 are look-ahead blocks (when a next pivot block
+// K' = [k1, k1+kb1) exists), one per 32 columns J: warps 0-3 form the next
+// pivot block D' = Mout[K',K'] from the inputs and invert it while warps 4-7
+// write the rows K' of Mout for the columns J; then all form
+// T' = D'^-1 Mout[K', J] (Tnext), and block 0 writes D'^-1 (invnext): the
+// next step needs no separate preparation launch, and the serial inversion
+// overlaps the bulk update.  The other blocks update the 16-row x 32-column
+// tiles of every other row band, taking tiles from a ticket counter (zero at
+// launch) until none are left.  256 threads.
+__global__ void __launch_bounds__(256) k_gj_step(const double *__restrict__ Min, double *__restrict__ Mout,
+                                                 int n, int k0, int kb,
+                                                 const double *__restrict__ Tcur,
+                                                 const double *__restrict__ invcur, int k1, int kb1,
+                                                 double *__restrict__ Tnext, double *__restrict__ invnext,
+                                                 int *err, unsigned long long *minpiv, double tol,
+                                                 int *__restrict__ ticket)
+{
+    __shared__ double sC[NB][NB + 1];
+    __shared__ double sT[NB][32];
+    __shared__ double sInv[NB][NB];
+    __shared__ double sOut[NB][33];
+    __shared__ double sA[2 * NB][NB + 1];
+    __shared__ double s_red[4];
+    const int t = threadIdx.x;
+    const int ncol = (n + 31) / 32;
+    const bool look = kb1 > 0;
+    const int nlook = look ? ncol : 0;
+    const int nband = (n + NB - 1) / NB;
+    const int nbulk = (nband - (look ? 1 : 0)) * ncol;
+    sInv[t >> 4][t & 15] = invcur[t];
+    if ((int)blockIdx.x >= nlook) {
+        // bulk: 16-row x 32-column tiles handed out by a ticket counter (every
+        // SM keeps working until the tiles run out), 2 columns per thread
+        __shared__ int s_tile;
+        for (;;) {
+            __syncthreads();
+            if (t == 0) s_tile = atomicAdd(ticket, 1);
+            __syncthreads();
+            const int b = s_tile;
+            if (b >= nbulk) return;
+            const int rb = b / ncol;
+            const int band = (look && rb >= k1 / NB) ? rb + 1 : rb;
+            const int jc = b - rb * ncol;
+            const int i0 = band * NB, j0 = jc * 32;
+            {
+                const int r = t >> 4, l = t & 15;
+                sC[r][l] = (i0 + r < n && l < kb) ? Min[(int64_t)(i0 + r) * n + k0 + l] : 0.0;
+                for (int u = t; u < NB * 32; u += 256) {
+                    const int k = u >> 5, cc = u & 31;
+                    sT[k][cc] = (j0 + cc < n) ? Tcur[(int64_t)k * n + j0 + cc] : 0.0;
+                }
+            }
+            __syncthreads();
+            const int r = t >> 4, c0 = (t & 15) * 2;
+            const int i = i0 + r;
+            if (i < n) {
+                double ci[NB];
 #pragma unroll
-    for (int u = 0; u < 4; u++) {
-        const int c = c0 + u, j = j0 + c;
-        if (j >= n) continue;
-        const bool jK = j >= k0 && j < k0 + kb;
-        double *dst = M + (int64_t)i * n + j;
-        if (iK) {
-            if (jK) *dst = sInv[i - k0][j - k0];
-            continue;                // the rest of the pivot rows: part 1
+                for (int l = 0; l < NB; l++) ci[l] = sC[r][l];
+#pragma unroll
+                for (int u = 0; u < 2; u++) {
+                    const int cc = c0 + u, j = j0 + cc;
+                    if (j < n) Mout[(int64_t)i * n + j] = gj_entry(Min, n, i, j, k0, kb, ci, sT, cc, sInv);
+                }
+            }
         }
-        if (jK) {
-            double s = 0.0;
+    }
+    // look-ahead block: band K', column chunk blockIdx.x
+    const int i0 = k1, j0 = blockIdx.x * 32;
+    {
+        const int r = t >> 4, l = t & 15;
+        sC[r][l] = (i0 + r < n && l < kb) ? Min[(int64_t)(i0 + r) * n + k0 + l] : 0.0;
+        for (int u = t; u < NB * 32; u += 256) {
+            const int k = u >> 5, cc = u & 31;
+            sT[k][cc] = (j0 + cc < n) ? Tcur[(int64_t)k * n + j0 + cc] : 0.0;
+        }
+    }
+    __syncthreads();
+    if (t < 128) {
+        // D' from the inputs: rows K' = this band, columns K' (their C rows are
+        // sC, their T columns read from Tcur)
+        for (int u = t; u < 2 * NB * NB; u += 128) {
+            const int cc = u / NB, rr = u % NB;
+            double v;
+            if (cc < NB) {
+                if (rr < kb1 && cc < kb1) {
+                    double ci[NB];
 #pragma unroll
-            for (int l = 0; l < NB; l++) s = fma(ci[l], sInv[l][j - k0], s);
-            *dst = -s;
-        } else {
-            double s = 0.0;
+                    for (int l = 0; l < NB; l++) ci[l] = sC[rr][l];
+                    const int j = k1 + cc;
+                    double acc = 0.0;
+                    const bool jK = j >= k0 && j < k0 + kb;
+                    if (jK) {
 #pragma unroll
-            for (int l = 0; l < NB; l++) s = fma(ci[l], sT[l][c], s);
-            *dst = *dst - s;
+                        for (int l = 0; l < NB; l++) acc = fma(ci[l], sInv[l][j - k0], acc);
+                        v = -acc;
+                    } else {
+#pragma unroll
+                        for (int l = 0; l < NB; l++) acc = fma(ci[l], Tcur[(int64_t)l * n + j], acc);
+                        v = Min[(int64_t)(k1 + rr) * n + j] - acc;
+                    }
+                } else {
+                    v = rr == cc ? 1.0 : 0.0;
+                }
+            } else {
+                v = (rr == cc - NB) ? 1.0 : 0.0;
+            }
+            sA[cc][rr] = v;
+        }
+        bar128();
+        const double rel = block_invert(sA, kb1, tol, s_red);
+        if (blockIdx.x == 0 && t == 0) {
+            if (rel < 0.0) atomicExch(err, 1);
+            else atomic_min_pos(minpiv, rel);
+        }
+    } else {
+        // rows K' of this chunk: 16 x 32 entries, 4 per thread
+        const int tt = t - 128;
+        const int r = tt >> 3, c0 = (tt & 7) * 4;
+        const int i = i0 + r;
+        double ci[NB];
+#pragma unroll
+        for (int l = 0; l < NB; l++) ci[l] = sC[r][l];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int cc = c0 + u, j = j0 + cc;
+            double out = 0.0;
+            if (i < n && j < n) {
+                out = gj_entry(Min, n, i, j, k0, kb, ci, sT, cc, sInv);
+                Mout[(int64_t)i * n + j] = out;
+            }
+            sOut[r][cc] = (r < kb1) ? out : 0.0;
+        }
+    }
+    __syncthreads();
+    if (blockIdx.x == 0)
+        for (int u = t; u < NB * NB; u += 256) invnext[u] = sA[NB + u % NB][u / NB];
+    // T' = D'^-1 rows K' for this chunk: 2 entries per thread
+    {
+        const int k = t >> 4, c0 = (t & 15) * 2;
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const int cc = c0 + u, j = j0 + cc;
+            if (j < n) {
+                double acc = 0.0;
+#pragma unroll
+                for (int l = 0; l < NB; l++) acc = fma(sA[NB + l][k], sOut[l][cc], acc);
+                Tnext[(int64_t)k * n + j] = acc;
+            }
         }
     }
 }
@@ -282,7 +405,11 @@ struct vefem_frontal {
     std::vector<int> n, p;
     const int32_t *ext = nullptr;   // caller's device arrays
     const int64_t *idx = nullptr;
-    double *Tbuf = nullptr, *Cbuf = nullptr, *inv = nullptr;
+    double *Tbuf[2] = {nullptr, nullptr}, *inv[2] = {nullptr, nullptr};
+    double *W = nullptr;                  // ping-pong partner of a panel's matrix
+    int *tickets = nullptr;               // one tile counter per Gauss-Jordan step
+    int64_t nsteps_total = 0;
+    int bulk_ctas = 0;                    // resident CTAs of the step kernel on this GPU
     int *err = nullptr;
     unsigned long long *minpiv = nullptr;
     unsigned long long h_minpiv = 0;   // staging of the initial value (outlives the async copy)
@@ -362,14 +489,27 @@ extern "C" int vefem_frontal_create(int device, int npan, const int64_t *off, co
         delete f;
         return VEFEM_ERR_ARG;
     }
+    for (int q = 0; q < npan; q++) f->nsteps_total += (p[q] + NB - 1) / NB;
     DeviceGuard g(device);
+    {
+        int sms = 0, occ = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_gj_step, 256, 0) != cudaSuccess) {
+            delete f;
+            return VEFEM_ERR_CUDA;
+        }
+        f->bulk_ctas = sms * std::max(1, occ);
+    }
     if (cudaMalloc(&f->wb, (size_t)N * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&f->wy, (size_t)N * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&f->wx, (size_t)N * sizeof(double)) != cudaSuccess ||
         cudaStreamCreateWithFlags(&f->cs, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaMalloc(&f->Tbuf, (size_t)NB * f->nmax * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&f->Cbuf, (size_t)NB * f->nmax * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&f->inv, NB * NB * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&f->Tbuf[0], (size_t)NB * f->nmax * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&f->Tbuf[1], (size_t)NB * f->nmax * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&f->inv[0], NB * NB * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&f->inv[1], NB * NB * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&f->W, (size_t)f->nmax * f->nmax * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&f->tickets, (size_t)std::max<int64_t>(1, f->nsteps_total) * sizeof(int)) != cudaSuccess ||
         cudaMalloc(&f->err, sizeof(int)) != cudaSuccess ||
         cudaMalloc(&f->minpiv, sizeof(unsigned long long)) != cudaSuccess) {
         vefem_frontal_destroy(f);
@@ -386,6 +526,8 @@ extern "C" int vefem_frontal_factor(vefem_frontal *f, double *buf, void *stream,
     DeviceGuard g(f->device);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     FCK(cudaMemsetAsync(f->err, 0, sizeof(int), s));
+    FCK(cudaMemsetAsync(f->tickets, 0, (size_t)f->nsteps_total * sizeof(int), s));
+    int64_t step_id = 0;
     const double d_one = 1.0;
     std::memcpy(&f->h_minpiv, &d_one, sizeof(d_one));
     FCK(cudaMemcpyAsync(f->minpiv, &f->h_minpiv, sizeof(f->h_minpiv), cudaMemcpyHostToDevice, s));
@@ -400,13 +542,29 @@ extern "C" int vefem_frontal_factor(vefem_frontal *f, double *buf, void *stream,
                     M, n, buf + f->off[q - 1], np, pp, f->ext + f->ext_off[q - 1], fr);
             }
         }
-        const unsigned gp = (unsigned)((n + 15) / 16);
-        const dim3 gu((unsigned)((n + TILE - 1) / TILE), (unsigned)((n + TILE - 1) / TILE));
-        for (int k0 = 0; k0 < p; k0 += NB) {
-            const int kb = std::min(NB, p - k0);
-            k_gj_prep<<<gp, 128, 0, s>>>(M, n, k0, kb, f->Tbuf, f->Cbuf, f->inv, f->err, f->minpiv, tol);
-            k_gj_update<<<gu, 256, 0, s>>>(M, n, k0, kb, f->Tbuf, f->Cbuf, f->inv);
+        if (p == 0) continue;
+        // Gauss-Jordan steps ping-pong between the panel's matrix and W
+        const int ncol = (n + 31) / 32, nband = (n + NB - 1) / NB;
+        const int nsteps = (p + NB - 1) / NB;
+        k_gj_start<<<(unsigned)ncol, 128, 0, s>>>(M, n, std::min(NB, p), f->Tbuf[0], f->inv[0], f->err,
+                                                  f->minpiv, tol);
+        for (int st = 0; st < nsteps; st++) {
+            const int k0 = st * NB, kb = std::min(NB, p - k0);
+            const int k1 = k0 + NB, kb1 = k1 < p ? std::min(NB, p - k1) : 0;
+            const double *Min = (st & 1) ? f->W : M;
+            double *Mout = (st & 1) ? M : f->W;
+            // look-ahead blocks (one per column chunk, when a next pivot block
+            // exists) + bulk blocks for every other row band
+            const int nlook = kb1 > 0 ? ncol : 0;
+            const int nbulk = (nband - (kb1 > 0 ? 1 : 0)) * ncol;
+            const int grid = nlook + std::max(1, std::min(nbulk, f->bulk_ctas - nlook));
+            k_gj_step<<<(unsigned)grid, 256, 0, s>>>(Min, Mout, n, k0, kb, f->Tbuf[st & 1],
+                                                     f->inv[st & 1], k1, kb1, f->Tbuf[(st + 1) & 1],
+                                                     f->inv[(st + 1) & 1], f->err, f->minpiv, tol,
+                                                     f->tickets + step_id);
+            step_id++;
         }
+        if (nsteps & 1) FCK(cudaMemcpyAsync(M, f->W, (size_t)n * n * sizeof(double), cudaMemcpyDeviceToDevice, s));
     }
     FCK(cudaGetLastError());
     int herr = 0;
@@ -486,9 +644,12 @@ extern "C" void vefem_frontal_destroy(vefem_frontal *f)
         cudaFree(f->wb);
         cudaFree(f->wy);
         cudaFree(f->wx);
-        cudaFree(f->Tbuf);
-        cudaFree(f->Cbuf);
-        cudaFree(f->inv);
+        cudaFree(f->Tbuf[0]);
+        cudaFree(f->Tbuf[1]);
+        cudaFree(f->inv[0]);
+        cudaFree(f->inv[1]);
+        cudaFree(f->W);
+        cudaFree(f->tickets);
         cudaFree(f->err);
         cudaFree(f->minpiv);
     }

@@ -161,11 +161,16 @@ __device__ void stab_base(const KParams &p, const double *tlb /* [9][10] */, con
         for (int j = 0; j < 3; j++) Gdtr[i][j] = GUtr[i][j] + GUTtr[i][j];
     // conEQ_* (Constitutive_Models_mod.F90:96-268), models restated for stability
     const double trT = tr3(S);
-    double fT = 1.0, f0 = 1.0, f1 = 1.0, f2 = 0.0, g0 = 1.0, g1 = 1.0;
+    const bool fene = p.model == FENE_CR || p.model == FENE_P;
+    double fT = 1.0, f0 = 1.0, f1 = 1.0, f2 = 0.0, g0 = 1.0, g1 = 1.0, termI = 0.0;
     if (p.model == L_PTT || p.model == M_L_PTT) {
         fT = 1.0 + (VeN * WiN * trT) / (1.0 - BvN);
     } else if (p.model == E_PTT || p.model == M_E_PTT) {
         fT = exp(VeN * WiN * trT / (1.0 - BvN));
+    } else if (p.model == FENE_CR) {   // N = 2, the base problem's dimension
+        fT = 1.0 + ((WiN * trT / (1.0 - BvN))) / (VeN - 2.0);
+    } else if (p.model == FENE_P) {
+        fT = 1.0 + (WiN * trT / (1.0 - BvN)) / VeN;
     } else {  // GIESEKUS
         fT = VeN * WiN / (1.0 - BvN);
     }
@@ -173,6 +178,22 @@ __device__ void stab_base(const KParams &p, const double *tlb /* [9][10] */, con
         f2 = fT;
     } else if (p.model == M_L_PTT || p.model == M_E_PTT) {
         f0 = fT; f1 = fT; g0 = fT; g1 = fT;
+    } else if (fene) {
+        // setFENEMaterialDerivative (steady): U . grad f_T from the trace of grad T
+        double df[3] = {0.0, 0.0, 0.0};
+        for (int i = 0; i < 3; i++)
+            for (int c = 0; c < 3; c++) df[c] = df[c] + dS[i][i][c];
+        const double den = p.model == FENE_P ? VeN : (VeN - 2.0);
+        for (int c = 0; c < 3; c++) df[c] = (WiN / (1.0 - BvN)) * df[c] / den;
+        double MD = 0.0;
+        for (int i = 0; i < 3; i++) MD = MD + U[i] * df[i];
+        f1 = fT - (WiN * MD / fT);
+        if (p.model == FENE_CR) {
+            f0 = fT; g0 = fT; g1 = fT;
+        } else {
+            g1 = fT;
+            termI = MD / fT;
+        }
     } else {
         f1 = fT;
     }
@@ -190,7 +211,7 @@ __device__ void stab_base(const KParams &p, const double *tlb /* [9][10] */, con
             const double ucd = UCD[i][j] - M1[i][j] - M2[i][j];
             double c = WiN * ucd + f2 * T2[i][j];
             c = c + f1 * S[i][j];
-            c = c - f0 * (1.0 - BvN) * (Gdtr[i][j] + 0.0);
+            c = c - f0 * (1.0 - BvN) * (Gdtr[i][j] + termI * (i == j ? 1.0 : 0.0));
             CE[i][j] = c;
         }
     // setStabilizationTerms
@@ -283,13 +304,40 @@ __device__ void stab_coef(const KParams &p, const StabBase &b, double K, int kz,
         for (int j = 0; j < 3; j++) GUT[i][j] = GU[j][i];
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++) Gd[i][j] = GU[i][j] + GUT[i][j];
-    // conEQ_*_Stability (Constitutive_Models_Stability_mod.F90:96-225)
+    // conEQ_*_Stability (Constitutive_Models_Stability_mod.F90:96-289)
     const double trT = tr3(S);
-    double fT = 0.0, f0 = 0.0, f1 = 0.0;
+    const bool fene = p.model == FENE_CR || p.model == FENE_P;
+    double fT = 0.0, f0 = 0.0, f1 = 0.0, termI = 0.0, termIt = 0.0;
     if (p.model == L_PTT || p.model == M_L_PTT) fT = VeN * WiN * trT / (1.0 - BvN);
     else if (p.model == E_PTT || p.model == M_E_PTT) fT = b.fT * VeN * WiN * trT / (1.0 - BvN);
-    if (p.model == M_L_PTT || p.model == M_E_PTT) f0 = fT;
+    else if (p.model == FENE_CR) fT = (WiN * trT / (1.0 - BvN)) / (VeN - 2.0);
+    else if (p.model == FENE_P) fT = (WiN * trT / (1.0 - BvN)) / VeN;
+    if (p.model == M_L_PTT || p.model == M_E_PTT || p.model == FENE_CR) f0 = fT;
     if (p.model != GIESEKUS) f1 = fT;
+    if (fene) {
+        // setFENEMaterialDerivativeStability (:294-328)
+        double dfb[3] = {0.0, 0.0, 0.0}, dfd[3] = {0.0, 0.0, 0.0};
+        for (int i = 0; i < 3; i++)
+            for (int c = 0; c < 3; c++) {
+                dfb[c] = dfb[c] + b.dT[i][i][c];
+                dfd[c] = dfd[c] + dT[i][i][c];
+            }
+        const double den = p.model == FENE_P ? VeN : (VeN - 2.0);
+        for (int c = 0; c < 3; c++) {
+            dfb[c] = (WiN / (1.0 - BvN)) * dfb[c] / den;
+            dfd[c] = (WiN / (1.0 - BvN)) * dfd[c] / den;
+        }
+        double MD = 0.0;
+        for (int i = 0; i < 3; i++) {
+            const double term = ((b.fT) * dfd[i] - fT * dfb[i]) / (b.fT);
+            MD = MD + U[i] * dfb[i] + b.U[i] * term;
+        }
+        f1 = fT - WiN * MD / (b.fT);
+        if (p.model == FENE_P) {
+            termI = MD / (b.fT);
+            termIt = -(1.0 - BvN) * fT / (b.fT);
+        }
+    }
     // setStressTensorStability: P_tot (C_Tensor of the perturbation is not used below)
     double Pt[3][3];
     for (int i = 0; i < 3; i++)
@@ -313,7 +361,7 @@ __device__ void stab_coef(const KParams &p, const StabBase &b, double K, int kz,
             const double tT = b.f[2] * (SbSd[i][j] + SdSb[i][j]) + 0.0 * SbSb[i][j] + f1 * b.S[i][j]
                               + b.f[1] * S[i][j];
             const double tG = b.f[0] * Gd[i][j] + f0 * b.G_dot[i][j];
-            CE[i][j] = WiN * ucd + tT - (1.0 - BvN) * tG;
+            CE[i][j] = WiN * ucd + tT - (1.0 - BvN) * (tG + termI * (i == j ? 1.0 : 0.0));
         }
     // strongFormMomentumStability
     double Mom[3], mt[3];
@@ -329,9 +377,13 @@ __device__ void stab_coef(const KParams &p, const StabBase &b, double K, int kz,
     }
     const double Cont = tr3(GU);
     const double magd = ddot(b.CE, CE) / (2.0 * b.mag + 1.0e-12);
-    double ceqt[3][3];
+    double ceqt[3][3];     // Con_EQ_time (strongFormConEQ_Stability :85-93)
     for (int i = 0; i < 3; i++)
-        for (int j = 0; j < 3; j++) ceqt[i][j] = WiN * S[i][j];
+        for (int j = 0; j < 3; j++) {
+            double c = WiN * S[i][j];
+            if (fene) c = c - WiN * fT * b.S[i][j] / (b.fT);
+            ceqt[i][j] = c + termIt * (i == j ? 1.0 : 0.0);
+        }
     double conv[3];
     for (int i = 0; i < 3; i++) {
         double c1 = 0.0, c2 = 0.0;
@@ -652,8 +704,6 @@ extern "C" int vefem_stability_assemble(vefem_ctx *ctx, const double *TLb, int n
         if (!A[k]) return sfail(ctx, VEFEM_ERR_ARG, "NULL A array");
     if (ctx->prm.form != FORM_T)
         return sfail(ctx, VEFEM_ERR_UNSUPPORTED, "stability assembly: T form only");
-    if (ctx->prm.model == FENE_CR || ctx->prm.model == FENE_P)
-        return sfail(ctx, VEFEM_ERR_UNSUPPORTED, "stability assembly: FENE models not restated");
     SCK(cudaSetDevice(ctx->device));
     if (int rc = stab_pattern(ctx)) return rc;
     cudaStream_t s = ctx->stream;
