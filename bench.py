@@ -97,7 +97,7 @@ def parse_args():
                          "(0 = skip it)")
     ap.add_argument("--newton-only", type=int, default=0, metavar="NEL",
                     help="only the precision-form Newton comparison (FP64 vs FP32 Jacobian, "
-                         "natural continuation Wi 0.1, 0.3, 0.5) on a mesh of NEL quads")
+                         "natural continuation Wi 0.1, 0.2, 0.3, 0.4, 0.5) on a mesh of NEL quads")
     ap.add_argument("--linear-solver", choices=["auto", "frontal", "superlu"], default="auto",
                     help="linear solver of the Newton and continuation legs (auto: the GPU "
                          "frontal LU from 1,000 elements on, host SuperLU below)")
@@ -454,7 +454,7 @@ def _solver_desc(solver) -> str:
     return "host SuperLU (nested dissection)"
 
 
-def newton_precision_compare(nel: int, device: int = 0, wis=(0.1, 0.3, 0.5),
+def newton_precision_compare(nel: int, device: int = 0, wis=(0.1, 0.2, 0.3, 0.4, 0.5),
                              linear_solver: str = "auto"):
     """Precision form on one Newton solve per Weissenberg number: Giesekus
     alpha = 0.1, beta = 0.59, SQRT form, natural continuation through ``wis``

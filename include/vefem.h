@@ -223,8 +223,12 @@ int vefem_abi_version(void);
  * then factorises with pivoting); min_pivot (may be NULL) receives the
  * smallest such ratio.  Synchronises the stream.
  * vefem_frontal_solve: x = A^-1 b with the factors in buf; b and x are device
- * vectors of N doubles (b is not modified).  The sweeps are captured once per
- * buf into a CUDA graph and replayed; asynchronous on the stream.
+ * vectors of N doubles (b is not modified).  The sweeps (two launches per
+ * panel, chained by programmatic dependent launch where the driver accepts it)
+ * are captured once per buf into a CUDA graph and replayed; asynchronous on
+ * the stream.
+ * vefem_frontal_solve_path: how the last solve's launches were chained (1
+ * programmatic dependent launch, 2 plain stream order; -1 no solve yet).
  * stream: a cudaStream_t (NULL = default stream). */
 typedef struct vefem_frontal vefem_frontal;
 
@@ -238,6 +242,7 @@ int vefem_frontal_solve(vefem_frontal *f, const double *buf, const double *b, do
                         void *stream);
 void vefem_frontal_destroy(vefem_frontal *f);
 const char *vefem_frontal_last_error(const vefem_frontal *f);
+int vefem_frontal_solve_path(const vefem_frontal *f);
 
 /* ---- Linear stability: batched A/B assembly --------------------------------
  * setEquationsBulkStability (Stability/Equations_Stability_mod.F90:20-226):

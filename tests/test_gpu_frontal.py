@@ -66,6 +66,7 @@ def test_native_frontal_matches_superlu_2000(jac, arclength):
     assert np.linalg.norm(x - x_ref) <= 1e-9 * np.linalg.norm(x_ref)
     # the same solve again: bit for bit (fixed summation order, no atomics)
     assert np.array_equal(lu.solve(b), x)
+    assert lu.solve_path in (1, 2)
     lu.close()
 
 

@@ -141,6 +141,43 @@ def test_add_semantics_and_determinism():
     asm.close()
 
 
+@pytest.mark.parametrize("jac", ["fd64", "exact32"])
+def test_zero_first_with_entries_outside_element_blocks(jac):
+    """A caller's pattern may hold node-row entries no element block covers
+    (here: the six columns of a distant node in the rows of node 0).  With
+    VEFEM_ZERO_FIRST they come back zero and every other entry equals the
+    assembly on the plain pattern, whatever the arrays held before."""
+    mesh = M.build_cylinder_mesh(2000)
+    phys = S.oldroyd_b(0.1, 0.59, "SQRT", nex=1)
+    TL, EU = S.seeded_state(mesh.xyz, phys, 4)
+    rowptr, colind = P.build_pattern(mesh.element_nodes(), mesh.nnodes, 1)
+    far = mesh.nnodes - 1
+    assert far * 6 not in set(colind[rowptr[0]:rowptr[1]])
+    rows = [list(colind[rowptr[r]:rowptr[r + 1]]) for r in range(len(rowptr) - 1)]
+    for r in range(6):
+        rows[r] = sorted(rows[r] + [far * 6 + q for q in range(6)])
+    rp2 = np.concatenate([[0], np.cumsum([len(c) for c in rows])]).astype(rowptr.dtype)
+    ci2 = np.concatenate(rows).astype(colind.dtype)
+    rng = np.random.default_rng(1)
+    out = {}
+    for name, (rp, ci) in (("plain", (rowptr, colind)), ("extra", (rp2, ci2))):
+        asm = V.BulkAssembler(mesh, phys, rp, ci)
+        b0 = rng.normal(size=len(rp) - 1)
+        v0 = rng.normal(size=len(ci)).astype(np.float64 if jac == "fd64" else np.float32)
+        b, v = asm.set_equations_bulk(TL, EU, "NRP", b=b0, vals=v0, zero_first=True, jacobian=jac)
+        asm.close()
+        out[name] = (rp, ci, b, v)
+    _, _, bp, vp = out["plain"]
+    _, _, be, ve = out["extra"]
+    assert np.array_equal(bp, be)
+    extra = np.zeros(len(ci2), dtype=bool)
+    for r in range(6):
+        cols = ci2[rp2[r]:rp2[r + 1]]
+        extra[rp2[r]:rp2[r + 1]] = (cols >= far * 6) & (cols < far * 6 + 6)
+    assert np.all(ve[extra] == 0)
+    assert np.array_equal(ve[~extra], vp)
+
+
 @pytest.mark.parametrize("form", ["T", "SQRT"])
 def test_outlet_edges_after_bulk(form):
     """Outlet open-BC edges (setEquationsEdge) added after the bulk, in edge order."""

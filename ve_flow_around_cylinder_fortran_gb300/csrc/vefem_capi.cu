@@ -383,6 +383,8 @@ extern "C" int vefem_create(const vefem_mesh *mesh, const vefem_csr *pat,
     }
     ctx->nblocks = nblocks;
     ctx->nedge = nedge;
+    ctx->node_nnz = rowptr[(int64_t)nn * 6];
+    ctx->blocks_cover = ctx->node_nnz == (int64_t)nblocks * 36 + (nex ? (int64_t)nn * 6 : 0);
     ctx->h_rowptr.assign(rowptr, rowptr + N + 1);
     ctx->h_colind.assign(colind, colind + rowptr[N]);
 
@@ -528,9 +530,20 @@ extern "C" int vefem_assemble(vefem_ctx *ctx, const double *TL, const double *EU
                 CK(cudaMemcpyAsync(dvals32, vals32, ctx->nnz * sizeof(float), cudaMemcpyHostToDevice, s));
         }
     }
-    if (flags & VEFEM_ZERO_FIRST) {
-        if (want_res) CK(cudaMemsetAsync(db, 0, ctx->N * sizeof(double), s));
-        if (want_jac) CK(cudaMemsetAsync(jac32 ? (void *)dvals32 : (void *)dvals, 0, ctx->nnz * vsize, s));
+    // VEFEM_ZERO_FIRST: the scatter writes the node rows' sums without reading
+    // them (they start from zero, the same bits as after a memset); only what
+    // it does not cover is cleared: the arclength rows, and every entry when
+    // the caller's pattern has node-row entries outside the element blocks
+    const bool zero_first = (flags & VEFEM_ZERO_FIRST) != 0;
+    const int64_t nrow_nodes = (int64_t)ctx->nnodes * 6;
+    if (zero_first) {
+        if (want_res && ctx->N > nrow_nodes)
+            CK(cudaMemsetAsync(db + nrow_nodes, 0, (ctx->N - nrow_nodes) * sizeof(double), s));
+        if (want_jac) {
+            const int64_t z0 = ctx->blocks_cover ? ctx->node_nnz : 0;
+            char *base = jac32 ? (char *)dvals32 : (char *)dvals;
+            if (ctx->nnz > z0) CK(cudaMemsetAsync(base + z0 * vsize, 0, (ctx->nnz - z0) * vsize, s));
+        }
     }
     if (timing) CK(cudaEventRecord(ctx->ev[1], s));
 
@@ -602,11 +615,13 @@ extern "C" int vefem_assemble(vefem_ctx *ctx, const double *TL, const double *EU
     ga.boff = ctx->d_boff;
     ga.bptr = ctx->d_bptr;
     ga.bcon = ctx->d_bcon;
+    ga.store = zero_first ? 1 : 0;
     if (want_res) {
         CK(launch_gather_residual(ga, ctx->d_rs, db, s));
         ctx->launches++;
     }
     if (timing) CK(cudaEventRecord(ctx->ev[3], s));
+    ga.store = zero_first && ctx->blocks_cover ? 1 : 0;
     if (want_jac && !jac32) {
         CK(launch_gather_jacobian(ga, ctx->d_es, dvals, s));
         ctx->launches++;

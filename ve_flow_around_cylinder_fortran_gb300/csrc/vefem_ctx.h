@@ -15,6 +15,8 @@ struct vefem_ctx {
     int64_t N = 0, nnz = 0;
     int nblocks = 0;
     int nedge = 0;
+    int64_t node_nnz = 0;       // AIJ entries of the node rows (rowptr[6 nnodes])
+    bool blocks_cover = false;  // element blocks + arclength column = every node-row entry
     vefem::KParams prm{};
     cudaStream_t stream = nullptr;
     cudaStream_t stream2 = nullptr;          // FP64 residual beside an exact Jacobian

@@ -30,8 +30,17 @@
 // Solve (two launches per panel, replayed from a CUDA graph): forward
 // y_P = A^-1 b_P, b_F += (-C A^-1) b_P; backward x_P = y_P - (A^-1 B) x_F.  Sums
 // run in a fixed order (warp-strided, then a fixed shuffle tree): results are
-// reproducible run to run.  (One launch of one 16-CTA cluster with cluster
-// barriers between panels measured slower: the FP64 rate of 16 SMs bounds it.)
+// reproducible run to run.  The sweeps are latency-bound (a panel's rows are a
+// few hundred dot products of a few hundred entries), so the vectors are kept
+// in elimination order (a panel's right-hand side is one contiguous slice,
+// staged in shared memory) and consecutive launches overlap by programmatic
+// dependent launch: each kernel loads its rows of the factors before it waits
+// for the previous one.  (Measured slower: one launch of one 16-CTA cluster
+// with cluster barriers between panels, bound by the FP64 rate of 16 SMs; and
+// one cooperative launch of all SMs whose CTAs ordered the panels through
+// per-panel counters in global memory, 29 ms against 21 ms per solve at
+// 20,000 quads: a counter handoff between SMs costs more than the hardware's
+// launch-to-launch dependency.)
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -360,38 +369,121 @@ __device__ double warp_sum(double s)
     return s;
 }
 
-// forward: row r of M[:, :p] against b_P; r < p -> y, r >= p -> b_F +=
-__global__ void k_solve_fwd(const double *__restrict__ M, int n, int p, const int64_t *__restrict__ idx,
-                            double *__restrict__ b, double *__restrict__ y)
+// Programmatic dependent launch: a sweep kernel is launched while the previous
+// one still runs; everything before pdl_wait() may read only what no kernel of
+// the solve writes (the factors and the index arrays), everything after it
+// sees the previous kernel's results.  Without a programmatic dependency the
+// wait returns at once.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_launch_dependents()
 {
-    const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+constexpr int SV_WARPS = 8;   // rows per CTA of the sweep kernels (a warp per row)
+constexpr int SV_PRE = 8;     // row entries per lane loaded before the wait
+
+// The sweeps work in elimination order: position start[q] + r holds the
+// unknown of panel q's pivot r, so a panel's right-hand side entries are one
+// contiguous slice; pidx[r] is the position of the panel's row r (its pivots
+// map to start + r, its front to the pivots of later panels).  Each row's sum
+// runs lane-strided over the columns, then a fixed shuffle tree.
+//
+// forward, panel q: row r of M[:, :p] against b_P; r < p -> y, r >= p -> b_F +=
+__global__ void __launch_bounds__(SV_WARPS * 32) k_solve_fwd(const double *__restrict__ M, int n, int p,
+                                                             int start, const int32_t *__restrict__ pidx,
+                                                             double *__restrict__ bp,
+                                                             double *__restrict__ y)
+{
+    extern __shared__ double s_vec[];
+    const int r = blockIdx.x * SV_WARPS + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
+    const double *row = M + (int64_t)(r < n ? r : 0) * n;
+    double pre[SV_PRE];
+#pragma unroll
+    for (int k = 0; k < SV_PRE; k++) {
+        const int c = lane + 32 * k;
+        pre[k] = (r < n && c < p) ? row[c] : 0.0;
+    }
+    const int dst = (r < n && r >= p) ? pidx[r] : start + r;
+    pdl_wait();
+    for (int c = threadIdx.x; c < p; c += blockDim.x) s_vec[c] = bp[start + c];
+    __syncthreads();
+    pdl_launch_dependents();
     if (r >= n) return;
-    const double *row = M + (int64_t)r * n;
     double s = 0.0;
-    for (int c = lane; c < p; c += 32) s = fma(row[c], b[idx[c]], s);
+#pragma unroll
+    for (int k = 0; k < SV_PRE; k++) {
+        const int c = lane + 32 * k;
+        if (c < p) s = fma(pre[k], s_vec[c], s);
+    }
+    for (int c = lane + 32 * SV_PRE; c < p; c += 32) s = fma(row[c], s_vec[c], s);
     s = warp_sum(s);
     if (lane == 0) {
         if (r < p)
-            y[idx[r]] = s;
+            y[dst] = s;
         else
-            b[idx[r]] += s;
+            bp[dst] += s;
     }
 }
 
-// backward: x_P = y_P - M[:p, p:] x_F
-__global__ void k_solve_bwd(const double *__restrict__ M, int n, int p, const int64_t *__restrict__ idx,
-                            const double *__restrict__ y, double *__restrict__ x)
+// backward, panel q: x_P = y_P - M[:p, p:] x_F
+__global__ void __launch_bounds__(SV_WARPS * 32) k_solve_bwd(const double *__restrict__ M, int n, int p,
+                                                             int start, const int32_t *__restrict__ pidx,
+                                                             const double *__restrict__ y,
+                                                             double *__restrict__ xp)
 {
-    const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    extern __shared__ double s_vec[];
+    const int r = blockIdx.x * SV_WARPS + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
-    if (r >= p) return;
-    const double *row = M + (int64_t)r * n + p;
     const int f = n - p;
+    const double *row = M + (int64_t)(r < p ? r : 0) * n + p;
+    double pre[SV_PRE];
+#pragma unroll
+    for (int k = 0; k < SV_PRE; k++) {
+        const int c = lane + 32 * k;
+        pre[k] = (r < p && c < f) ? row[c] : 0.0;
+    }
+    int src[SV_PRE];
+#pragma unroll
+    for (int k = 0; k < SV_PRE; k++) {
+        const int c = threadIdx.x + k * SV_WARPS * 32;
+        src[k] = c < f ? pidx[p + c] : 0;
+    }
+    pdl_wait();
+#pragma unroll
+    for (int k = 0; k < SV_PRE; k++) {
+        const int c = threadIdx.x + k * SV_WARPS * 32;
+        if (c < f) s_vec[c] = xp[src[k]];
+    }
+    for (int c = threadIdx.x + SV_PRE * SV_WARPS * 32; c < f; c += blockDim.x) s_vec[c] = xp[pidx[p + c]];
+    __syncthreads();
+    pdl_launch_dependents();
+    if (r >= p) return;
     double s = 0.0;
-    for (int c = lane; c < f; c += 32) s = fma(row[c], x[idx[p + c]], s);
+#pragma unroll
+    for (int k = 0; k < SV_PRE; k++) {
+        const int c = lane + 32 * k;
+        if (c < f) s = fma(pre[k], s_vec[c], s);
+    }
+    for (int c = lane + 32 * SV_PRE; c < f; c += 32) s = fma(row[c], s_vec[c], s);
     s = warp_sum(s);
-    if (lane == 0) x[idx[r]] = y[idx[r]] - s;
+    if (lane == 0) xp[start + r] = y[start + r] - s;
+}
+
+// b in elimination order (bp[i] = b[elim[i]]), and back (x[elim[i]] = xp[i])
+__global__ void k_to_elim(int64_t N, const int32_t *__restrict__ elim, const double *__restrict__ b,
+                          double *__restrict__ bp)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < N) bp[i] = b[elim[i]];
+}
+
+__global__ void k_from_elim(int64_t N, const int32_t *__restrict__ elim, const double *__restrict__ xp,
+                            double *__restrict__ x)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < N) x[elim[i]] = xp[i];
 }
 
 }  // namespace
@@ -413,8 +505,15 @@ struct vefem_frontal {
     int *err = nullptr;
     unsigned long long *minpiv = nullptr;
     unsigned long long h_minpiv = 0;   // staging of the initial value (outlives the async copy)
-    // solve: work vectors and the CUDA graph of the two sweeps (captured per buf)
+    // solve: work vectors in elimination order and the CUDA graph of the two
+    // sweeps (captured per buf)
     double *wb = nullptr, *wy = nullptr, *wx = nullptr;
+    int32_t *elim = nullptr;              // global unknown at each elimination position
+    int32_t *pidx = nullptr;              // elimination position of every panel row (idx layout)
+    std::vector<int> start;               // first elimination position of each panel's pivots
+    int max_p = 0, max_f = 0;
+    bool pdl = true;                      // sweeps chained by programmatic dependent launch
+    int last_path = -1;                   // 1 graph with PDL, 2 graph without
     cudaStream_t cs = nullptr;
     cudaGraphExec_t graph = nullptr;
     const double *graph_buf = nullptr;
@@ -515,6 +614,59 @@ extern "C" int vefem_frontal_create(int device, int npan, const int64_t *off, co
         vefem_frontal_destroy(f);
         return VEFEM_ERR_NOMEM;
     }
+    // elimination order of the solve: panel q's pivots at start[q] .. start[q] + p[q]
+    {
+        if (N >= INT32_MAX || f->idx_off[npan] >= INT32_MAX) {
+            vefem_frontal_destroy(f);
+            return VEFEM_ERR_ARG;
+        }
+        std::vector<int64_t> hidx((size_t)f->idx_off[npan]);
+        if (cudaMemcpy(hidx.data(), idx, hidx.size() * sizeof(int64_t), cudaMemcpyDeviceToHost) != cudaSuccess) {
+            vefem_frontal_destroy(f);
+            return VEFEM_ERR_CUDA;
+        }
+        std::vector<int32_t> elim((size_t)N, -1), pos((size_t)N, -1), pidx(hidx.size());
+        f->start.resize(npan);
+        int64_t at = 0;
+        bool ok = true;
+        for (int q = 0; q < npan && ok; q++) {
+            f->start[q] = (int)at;
+            f->max_p = std::max(f->max_p, p[q]);
+            f->max_f = std::max(f->max_f, n[q] - p[q]);
+            for (int r = 0; r < p[q]; r++, at++) {
+                const int64_t g = hidx[(size_t)(f->idx_off[q] + r)];
+                if (g < 0 || g >= N || pos[(size_t)g] >= 0) { ok = false; break; }
+                pos[(size_t)g] = (int32_t)at;
+                elim[(size_t)at] = (int32_t)g;
+            }
+        }
+        for (size_t k = 0; ok && k < hidx.size(); k++) {
+            const int64_t g = hidx[k];
+            if (g < 0 || g >= N) { ok = false; break; }
+            pidx[k] = pos[(size_t)g];
+        }
+        if (!ok) {             // an unknown outside [0, N) or a pivot of two panels
+            vefem_frontal_destroy(f);
+            return VEFEM_ERR_ARG;
+        }
+        if (cudaMalloc(&f->elim, elim.size() * sizeof(int32_t)) != cudaSuccess ||
+            cudaMalloc(&f->pidx, pidx.size() * sizeof(int32_t)) != cudaSuccess) {
+            vefem_frontal_destroy(f);
+            return VEFEM_ERR_NOMEM;
+        }
+        if (cudaMemcpy(f->elim, elim.data(), elim.size() * sizeof(int32_t), cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(f->pidx, pidx.data(), pidx.size() * sizeof(int32_t), cudaMemcpyHostToDevice) != cudaSuccess) {
+            vefem_frontal_destroy(f);
+            return VEFEM_ERR_CUDA;
+        }
+        const size_t smem = (size_t)std::max(f->max_p, f->max_f) * sizeof(double);
+        if (smem > 48 * 1024 &&
+            (cudaFuncSetAttribute(k_solve_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+             cudaFuncSetAttribute(k_solve_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)) {
+            vefem_frontal_destroy(f);
+            return VEFEM_ERR_ARG;
+        }
+    }
     *out = f;
     return VEFEM_OK;
 }
@@ -579,21 +731,70 @@ extern "C" int vefem_frontal_factor(vefem_frontal *f, double *buf, void *stream,
 
 namespace {
 
-// the two sweeps of a solve, on stream s, with the handle's work vectors
-void launch_sweeps(vefem_frontal *f, const double *buf, cudaStream_t s)
+// One sweep launch; with pdl, the launch may begin while the previous kernel
+// on the stream still runs (programmatic stream serialisation).
+template <typename... Args, typename... Act>
+cudaError_t launch_sweep(bool pdl, void (*kern)(Args...), unsigned grid, size_t smem, cudaStream_t s,
+                         Act... args)
 {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(SV_WARPS * 32);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
+// the two sweeps of a solve in elimination order (wb -> wy -> wx), on stream s
+cudaError_t launch_sweeps(vefem_frontal *f, const double *buf, cudaStream_t s, bool pdl)
+{
+    const size_t smem_f = (size_t)std::max(1, f->max_p) * sizeof(double);
+    const size_t smem_b = (size_t)std::max(1, f->max_f) * sizeof(double);
     for (int q = 0; q < f->npan; q++) {
-        const int n = f->n[q];
-        if (f->p[q] == 0) continue;
-        k_solve_fwd<<<(unsigned)((n + 7) / 8), 256, 0, s>>>(buf + f->off[q], n, f->p[q],
-                                                           f->idx + f->idx_off[q], f->wb, f->wy);
+        const int n = f->n[q], p = f->p[q];
+        if (p == 0) continue;
+        const cudaError_t e = launch_sweep(pdl, k_solve_fwd, (unsigned)((n + SV_WARPS - 1) / SV_WARPS), smem_f,
+                                           s, (const double *)(buf + f->off[q]), n, p, f->start[q],
+                                           (const int32_t *)(f->pidx + f->idx_off[q]), f->wb, f->wy);
+        if (e != cudaSuccess) return e;
     }
     for (int q = f->npan - 1; q >= 0; q--) {
-        const int p = f->p[q];
+        const int n = f->n[q], p = f->p[q];
         if (p == 0) continue;
-        k_solve_bwd<<<(unsigned)((p + 7) / 8), 256, 0, s>>>(buf + f->off[q], f->n[q], p,
-                                                           f->idx + f->idx_off[q], f->wy, f->wx);
+        const cudaError_t e = launch_sweep(pdl, k_solve_bwd, (unsigned)((p + SV_WARPS - 1) / SV_WARPS), smem_b,
+                                           s, (const double *)(buf + f->off[q]), n, p, f->start[q],
+                                           (const int32_t *)(f->pidx + f->idx_off[q]),
+                                           (const double *)f->wy, f->wx);
+        if (e != cudaSuccess) return e;
     }
+    return cudaSuccess;
+}
+
+// capture the sweeps into f->graph; cudaSuccess or the first error
+cudaError_t capture_sweeps(vefem_frontal *f, const double *buf, bool pdl)
+{
+    cudaError_t e = cudaStreamBeginCapture(f->cs, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    const cudaError_t le = launch_sweeps(f, buf, f->cs, pdl);
+    cudaGraph_t gr = nullptr;
+    e = cudaStreamEndCapture(f->cs, &gr);
+    if (le != cudaSuccess || e != cudaSuccess) {
+        if (gr) cudaGraphDestroy(gr);
+        cudaGetLastError();
+        return le != cudaSuccess ? le : e;
+    }
+    e = cudaGraphInstantiate(&f->graph, gr, 0);
+    cudaGraphDestroy(gr);
+    if (e != cudaSuccess) {
+        f->graph = nullptr;
+        cudaGetLastError();
+    }
+    return e;
 }
 
 }  // namespace
@@ -604,34 +805,36 @@ extern "C" int vefem_frontal_solve(vefem_frontal *f, const double *buf, const do
     if (!f || !buf || !b || !x) return VEFEM_ERR_ARG;
     DeviceGuard g(f->device);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const unsigned pg = (unsigned)((f->N + 255) / 256);
     if (!f->graph || f->graph_buf != buf) {
         // capture the 2 x npan launches once per factor buffer: a replay costs a
-        // fraction of their launch overhead
+        // fraction of their launch overhead.  Chained by programmatic dependent
+        // launch where the driver accepts it, plain stream order otherwise.
         if (f->graph) {
             cudaGraphExecDestroy(f->graph);
             f->graph = nullptr;
         }
-        FCK(cudaStreamBeginCapture(f->cs, cudaStreamCaptureModeThreadLocal));
-        launch_sweeps(f, buf, f->cs);
-        cudaGraph_t gr = nullptr;
-        const cudaError_t le = cudaGetLastError();
-        FCK(cudaStreamEndCapture(f->cs, &gr));
-        if (le != cudaSuccess) {
-            cudaGraphDestroy(gr);
-            return ffail(f, VEFEM_ERR_CUDA, std::string("solve capture: ") + cudaGetErrorString(le));
+        cudaError_t e = f->pdl ? capture_sweeps(f, buf, true) : cudaErrorNotSupported;
+        if (e != cudaSuccess) {
+            f->pdl = false;
+            e = capture_sweeps(f, buf, false);
         }
-        const cudaError_t ie = cudaGraphInstantiate(&f->graph, gr, 0);
-        cudaGraphDestroy(gr);
-        if (ie != cudaSuccess) {
-            f->graph = nullptr;
-            return ffail(f, VEFEM_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie));
-        }
+        if (e != cudaSuccess)
+            return ffail(f, VEFEM_ERR_CUDA, std::string("solve graph: ") + cudaGetErrorString(e));
         f->graph_buf = buf;
     }
-    FCK(cudaMemcpyAsync(f->wb, b, (size_t)f->N * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    k_to_elim<<<pg, 256, 0, s>>>(f->N, f->elim, b, f->wb);
+    FCK(cudaGetLastError());
     FCK(cudaGraphLaunch(f->graph, s));
-    FCK(cudaMemcpyAsync(x, f->wx, (size_t)f->N * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    k_from_elim<<<pg, 256, 0, s>>>(f->N, f->elim, f->wx, x);
+    FCK(cudaGetLastError());
+    f->last_path = f->pdl ? 1 : 2;
     return VEFEM_OK;
+}
+
+extern "C" int vefem_frontal_solve_path(const vefem_frontal *f)
+{
+    return f ? f->last_path : -1;
 }
 
 extern "C" void vefem_frontal_destroy(vefem_frontal *f)
@@ -652,6 +855,8 @@ extern "C" void vefem_frontal_destroy(vefem_frontal *f)
         cudaFree(f->tickets);
         cudaFree(f->err);
         cudaFree(f->minpiv);
+        cudaFree(f->elim);
+        cudaFree(f->pidx);
     }
     delete f;
 }

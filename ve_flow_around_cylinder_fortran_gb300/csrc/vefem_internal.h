@@ -79,6 +79,8 @@ struct GatherArgs {
     const int32_t *boff;       // [nblocks] column offset of the block inside its rows
     const int32_t *bptr;       // [nblocks+1]
     const int32_t *bcon;       // contributor = e*81 + jnod*9 + inod, element order
+    int store = 0;             // 1: the sums start from zero (VEFEM_ZERO_FIRST), the
+                               // destination is written without being read
 };
 cudaError_t launch_gather_residual(const GatherArgs &g, const double *rs, double *b,
                                    cudaStream_t s);

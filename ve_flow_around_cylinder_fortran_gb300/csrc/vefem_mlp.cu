@@ -5,10 +5,10 @@
 // nearest even) in the forward and backward products, with FP32
 // accumulation; activations, gradients and the optimiser state are FP32.
 // GELU is the erf form, 0.5 x (1 + erf(x / sqrt 2)).  The loss is the mean
-// squared error over all outputs.  Batches are a few hundred rows at most, so
-// the products are plain tiled kernels on the CUDA cores; one training
-// iteration (forward, backward, Adam) is captured once in a CUDA graph and
-// replayed.
+// squared error over all outputs.  The products run on the tensor cores
+// (mma.sync BF16 with FP32 accumulation; FP32 operands as exact sums of three
+// BF16 terms, see k_linear_mma); one training iteration (forward, backward,
+// Adam) is captured once in a CUDA graph and replayed.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <math.h>
@@ -24,8 +24,6 @@
 
 namespace {
 
-constexpr int TILE = 16;
-
 struct Layer {
     int in, out;
     float *W = nullptr, *b = nullptr;          // FP32 master [out][in], [out]
@@ -36,30 +34,164 @@ struct Layer {
     float *dA = nullptr;                       // gradient w.r.t. A [n][out]
 };
 
-// Y[n][out] = X[n][in] . W^T + b, optional GELU; Z keeps the pre-activation
-__global__ void k_linear_fwd(const float *__restrict__ X, int n, int in,
-                             const __nv_bfloat16 *__restrict__ W, const float *__restrict__ b,
-                             int out, float *__restrict__ Z, float *__restrict__ A, int gelu)
+// ---- products on the tensor cores: mma.sync m16n8k16, BF16 x BF16 -> FP32
+//
+// The weights enter as their BF16 copy.  The activations and gradients are
+// FP32; each is split exactly into three BF16 terms (x = h + m + l: h the
+// nearest BF16, m the nearest BF16 of x - h, l of what is left; 8 + 8 + 8
+// significand bits cover FP32's 24), so with the exact BF16 x BF16 products
+// and FP32 accumulation a product X W^T is the FP32 product of the FP32
+// activations with the BF16 weights, as on the CUDA cores.  For the weight
+// gradient dZ^T X both operands are FP32: the six split products whose
+// magnitude exceeds 2^-24 of the leading one are summed (h h, h m, m h, h l,
+// l h, m m).  No atomics: every output is owned by one CTA, results are the
+// same on every run.
+//
+// The products are small (a few hundred rows by 256) and run once per
+// training iteration, so they are latency-bound: a CTA computes one 16 x 8
+// output tile, its four warps split K and their partial tiles are added in
+// warp order through shared memory.  Fragment layouts of m16n8k16
+// (g = lane / 4, t = lane % 4): A registers (g, 2t..2t+1), (g+8, 2t..),
+// (g, 2t+8..), (g+8, 2t+8..); B registers (k = 2t..2t+1, n = g),
+// (k = 2t+8.., n = g); C (g, 2t..2t+1), (g+8, 2t..2t+1).  Two BF16 per 32-bit
+// register, the lower index in the low half.
+constexpr int MMA_WARPS = 4;
+
+__device__ __forceinline__ uint32_t pack2(__nv_bfloat16 lo, __nv_bfloat16 hi)
 {
-    __shared__ float sx[TILE][TILE + 1], sw[TILE][TILE + 1];
-    const int r = blockIdx.y * TILE + threadIdx.y;     // sample
-    const int c = blockIdx.x * TILE + threadIdx.x;     // output unit
-    float acc = 0.0f;
-    for (int k0 = 0; k0 < in; k0 += TILE) {
-        const int kx = k0 + threadIdx.x, kw = k0 + threadIdx.y;
-        sx[threadIdx.y][threadIdx.x] = (r < n && kx < in) ? X[(size_t)r * in + kx] : 0.0f;
-        const int wc = blockIdx.x * TILE + threadIdx.x;
-        sw[threadIdx.y][threadIdx.x] =
-            (wc < out && kw < in) ? __bfloat162float(W[(size_t)wc * in + kw]) : 0.0f;
-        __syncthreads();
+    return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+}
+
+__device__ __forceinline__ void split3(float x, __nv_bfloat16 (&p)[3])
+{
+    p[0] = __float2bfloat16_rn(x);
+    const float r1 = x - __bfloat162float(p[0]);
+    p[1] = __float2bfloat16_rn(r1);
+    p[2] = __float2bfloat16_rn(r1 - __bfloat162float(p[1]));
+}
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1)
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+        "{%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, {%0, %1, %2, %3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+enum { LIN_FWD = 0, LIN_BWD_X = 1, LIN_BWD_W = 2 };
+
+// Operand element loaders (zero outside the matrix).
+//   forward  Y = X W^T:   A(m, k) = X[m][k]   (n x in),  B(k, c) = W[c][k]
+//   backward dX = dZ W:   A(m, k) = dZ[m][k]  (n x out), B(k, c) = W[k][c]
+//   weights  gW = dZ^T X: A(m, k) = dZ[k][m]  (out x n), B(k, c) = X[k][c], and
+//                         column c = in the constant 1 (its output is gb)
+template <int MODE>
+__device__ __forceinline__ float load_a(const float *__restrict__ A, int M, int K, int lda, int m, int k)
+{
+    if (m >= M || k >= K) return 0.0f;
+    return MODE == LIN_BWD_W ? A[(size_t)k * lda + m] : A[(size_t)m * lda + k];
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(MMA_WARPS * 32)
+k_linear_mma(int M, int N, int K, const float *__restrict__ A, int lda,
+             const __nv_bfloat16 *__restrict__ Wb, const float *__restrict__ Bf, int ldb,
+             const float *__restrict__ bias, float *__restrict__ out0, float *__restrict__ out1,
+             float *__restrict__ out2, int ldo, int gelu)
+{
+    __shared__ float s_part[MMA_WARPS - 1][32][4];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int g = lane >> 2, t = lane & 3;
+    const int m0 = blockIdx.y * 16, n0 = blockIdx.x * 8;
+    const int ksteps = (K + 15) / 16;
+    const int per = (ksteps + MMA_WARPS - 1) / MMA_WARPS;
+    const int ks1 = min(ksteps, (warp + 1) * per);
+    const int c = n0 + g;                  // the B column this thread loads
+    float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll 2
+    for (int ks = warp * per; ks < ks1; ks++) {
+        const int k0 = ks * 16;
+        // A fragments of the three split terms
+        uint32_t af[3][4];
+        {
+            const int rows[4] = {m0 + g, m0 + g + 8, m0 + g, m0 + g + 8};
+            const int cols[4] = {k0 + 2 * t, k0 + 2 * t, k0 + 2 * t + 8, k0 + 2 * t + 8};
 #pragma unroll
-        for (int k = 0; k < TILE; k++) acc += sx[threadIdx.y][k] * sw[k][threadIdx.x];
-        __syncthreads();
+            for (int r = 0; r < 4; r++) {
+                __nv_bfloat16 lo[3], hi[3];
+                split3(load_a<MODE>(A, M, K, lda, rows[r], cols[r]), lo);
+                split3(load_a<MODE>(A, M, K, lda, rows[r], cols[r] + 1), hi);
+#pragma unroll
+                for (int q = 0; q < 3; q++) af[q][r] = pack2(lo[q], hi[q]);
+            }
+        }
+        const int ks_[4] = {k0 + 2 * t, k0 + 2 * t + 1, k0 + 2 * t + 8, k0 + 2 * t + 9};
+        if (MODE != LIN_BWD_W) {
+            __nv_bfloat16 w[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int k = ks_[u];
+                const bool in = c < N && k < K;
+                w[u] = in ? (MODE == LIN_FWD ? Wb[(size_t)c * ldb + k] : Wb[(size_t)k * ldb + c])
+                          : __float2bfloat16_rn(0.0f);
+            }
+            const uint32_t b0 = pack2(w[0], w[1]), b1 = pack2(w[2], w[3]);
+            // small terms first
+            mma_bf16(acc, af[2], b0, b1);
+            mma_bf16(acc, af[1], b0, b1);
+            mma_bf16(acc, af[0], b0, b1);
+        } else {
+            __nv_bfloat16 x[4][3];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int k = ks_[u];
+                float v = 0.0f;
+                if (k < K && c < N) v = c < N - 1 ? Bf[(size_t)k * ldb + c] : 1.0f;
+                split3(v, x[u]);
+            }
+            uint32_t bf[3][2];
+#pragma unroll
+            for (int q = 0; q < 3; q++) {
+                bf[q][0] = pack2(x[0][q], x[1][q]);
+                bf[q][1] = pack2(x[2][q], x[3][q]);
+            }
+            mma_bf16(acc, af[1], bf[1][0], bf[1][1]);
+            mma_bf16(acc, af[2], bf[0][0], bf[0][1]);
+            mma_bf16(acc, af[0], bf[2][0], bf[2][1]);
+            mma_bf16(acc, af[1], bf[0][0], bf[0][1]);
+            mma_bf16(acc, af[0], bf[1][0], bf[1][1]);
+            mma_bf16(acc, af[0], bf[0][0], bf[0][1]);
+        }
     }
-    if (r < n && c < out) {
-        const float z = acc + b[c];
-        Z[(size_t)r * out + c] = z;
-        A[(size_t)r * out + c] = gelu ? 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)) : z;
+    // partial tiles of warps 1..3 added to warp 0's, in warp order
+    if (warp > 0) {
+#pragma unroll
+        for (int u = 0; u < 4; u++) s_part[warp - 1][lane][u] = acc[u];
+    }
+    __syncthreads();
+    if (warp != 0) return;
+#pragma unroll
+    for (int w = 0; w < MMA_WARPS - 1; w++)
+#pragma unroll
+        for (int u = 0; u < 4; u++) acc[u] += s_part[w][lane][u];
+    // epilogue
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+        const int m = m0 + g + (u >= 2 ? 8 : 0);
+        const int cc = n0 + 2 * t + (u & 1);
+        if (m >= M || cc >= N) continue;
+        const float v = acc[u];
+        if (MODE == LIN_FWD) {
+            const float z = v + bias[cc];
+            out0[(size_t)m * ldo + cc] = z;
+            out1[(size_t)m * ldo + cc] = gelu ? 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)) : z;
+        } else if (MODE == LIN_BWD_X) {
+            out0[(size_t)m * ldo + cc] = v;
+        } else {
+            if (cc < N - 1) out0[(size_t)m * ldo + cc] = v;
+            else out2[m] = v;
+        }
     }
 }
 
@@ -74,50 +206,9 @@ __global__ void k_gelu_bwd(int count, const float *__restrict__ Z, float *__rest
     dA[i] = dA[i] * (cdf + z * pdf);
 }
 
-// dX[n][in] = dZ[n][out] . W[out][in]
-__global__ void k_linear_bwd_x(const float *__restrict__ dZ, int n, int out,
-                               const __nv_bfloat16 *__restrict__ W, int in,
-                               float *__restrict__ dX)
+dim3 mma_grid(int M, int N)
 {
-    __shared__ float sd[TILE][TILE + 1], sw[TILE][TILE + 1];
-    const int r = blockIdx.y * TILE + threadIdx.y;
-    const int c = blockIdx.x * TILE + threadIdx.x;     // input unit
-    float acc = 0.0f;
-    for (int k0 = 0; k0 < out; k0 += TILE) {
-        const int kd = k0 + threadIdx.x, kw = k0 + threadIdx.y;
-        sd[threadIdx.y][threadIdx.x] = (r < n && kd < out) ? dZ[(size_t)r * out + kd] : 0.0f;
-        sw[threadIdx.y][threadIdx.x] =
-            (c < in && kw < out) ? __bfloat162float(W[(size_t)kw * in + c]) : 0.0f;
-        __syncthreads();
-#pragma unroll
-        for (int k = 0; k < TILE; k++) acc += sd[threadIdx.y][k] * sw[k][threadIdx.x];
-        __syncthreads();
-    }
-    if (r < n && c < in) dX[(size_t)r * in + c] = acc;
-}
-
-// gW[out][in] = dZ^T . X, gb[out] = sum over samples of dZ
-__global__ void k_linear_bwd_w(const float *__restrict__ dZ, const float *__restrict__ X, int n,
-                               int out, int in, float *__restrict__ gW, float *__restrict__ gb)
-{
-    __shared__ float sd[TILE][TILE + 1], sx[TILE][TILE + 1];
-    const int o = blockIdx.y * TILE + threadIdx.y;
-    const int c = blockIdx.x * TILE + threadIdx.x;
-    float acc = 0.0f, accb = 0.0f;
-    for (int k0 = 0; k0 < n; k0 += TILE) {
-        const int kd = k0 + threadIdx.x, kx = k0 + threadIdx.y;
-        sd[threadIdx.y][threadIdx.x] = (o < out && kd < n) ? dZ[(size_t)kd * out + o] : 0.0f;
-        sx[threadIdx.y][threadIdx.x] = (c < in && kx < n) ? X[(size_t)kx * in + c] : 0.0f;
-        __syncthreads();
-#pragma unroll
-        for (int k = 0; k < TILE; k++) {
-            acc += sd[threadIdx.y][k] * sx[k][threadIdx.x];
-            accb += sd[threadIdx.y][k];
-        }
-        __syncthreads();
-    }
-    if (o < out && c < in) gW[(size_t)o * in + c] = acc;
-    if (o < out && blockIdx.x == 0 && threadIdx.x == 0) gb[o] = accb;
+    return dim3((unsigned)((N + 7) / 8), (unsigned)((M + 15) / 16));
 }
 
 // MSE loss and its gradient: dY = 2 (Y - T) / (n out), *loss = mean (Y - T)^2.
@@ -246,9 +337,10 @@ void launch_forward(vefem_mlp *m, int n)
     const float *x = m->X;
     for (size_t i = 0; i < m->L.size(); i++) {
         Layer &l = m->L[i];
-        dim3 bs(TILE, TILE), gs((l.out + TILE - 1) / TILE, (n + TILE - 1) / TILE);
-        k_linear_fwd<<<gs, bs, 0, m->s>>>(x, n, l.in, l.Wb, l.b, l.out, l.Z, l.A,
-                                          i + 1 < m->L.size() ? 1 : 0);
+        // Y[n][out] = X[n][in] W^T + b (GELU but on the last layer); Z keeps the pre-activation
+        k_linear_mma<LIN_FWD><<<mma_grid(n, l.out), MMA_WARPS * 32, 0, m->s>>>(
+            n, l.out, l.in, x, l.in, l.Wb, nullptr, l.in, l.b, l.Z, l.A, nullptr, l.out,
+            i + 1 < m->L.size() ? 1 : 0);
         x = l.A;
     }
 }
@@ -261,11 +353,15 @@ void launch_backward(vefem_mlp *m, int n)
         if (i + 1 < (int)m->L.size())
             k_gelu_bwd<<<(n * l.out + 255) / 256, 256, 0, m->s>>>(n * l.out, l.Z, l.dA);
         const float *xin = i == 0 ? m->X : m->L[i - 1].A;
-        dim3 bs(TILE, TILE), gw((l.in + TILE - 1) / TILE, (l.out + TILE - 1) / TILE);
-        k_linear_bwd_w<<<gw, bs, 0, m->s>>>(l.dA, xin, n, l.out, l.in, l.gW, l.gb);
+        // gW[out][in] = dZ^T X and gb[out] = dZ^T 1 (the extra column)
+        k_linear_mma<LIN_BWD_W><<<mma_grid(l.out, l.in + 1), MMA_WARPS * 32, 0, m->s>>>(
+            l.out, l.in + 1, n, l.dA, l.out, nullptr, xin, l.in, nullptr, l.gW, nullptr, l.gb,
+            l.in, 0);
         if (i > 0) {
-            dim3 gx((l.in + TILE - 1) / TILE, (n + TILE - 1) / TILE);
-            k_linear_bwd_x<<<gx, bs, 0, m->s>>>(l.dA, n, l.out, l.Wb, l.in, m->L[i - 1].dA);
+            // dX[n][in] = dZ[n][out] W[out][in]
+            k_linear_mma<LIN_BWD_X><<<mma_grid(n, l.in), MMA_WARPS * 32, 0, m->s>>>(
+                n, l.in, l.out, l.dA, l.out, l.Wb, nullptr, l.in, nullptr, m->L[i - 1].dA,
+                nullptr, nullptr, l.in, 0);
         }
     }
 }

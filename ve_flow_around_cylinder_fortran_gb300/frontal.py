@@ -252,6 +252,14 @@ class FrontalLU:
             raise V.VefemError(f"vefem_frontal_create failed ({rc})")
         self._handle = h
 
+    @property
+    def solve_path(self):
+        """How the last native solve's launches were chained: 1 programmatic
+        dependent launch, 2 plain stream order, -1 no solve yet."""
+        if self._handle is None:
+            return -1
+        return int(self._L.vefem_frontal_solve_path(self._handle))
+
     def close(self):
         if self._handle is not None:
             self._L.vefem_frontal_destroy(self._handle)

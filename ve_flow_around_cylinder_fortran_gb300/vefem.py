@@ -41,7 +41,7 @@ EXPORTED = ["vefem_abi_version", "vefem_create", "vefem_set_params", "vefem_asse
             "vefem_batch_last_timing", "vefem_batch_destroy", "vefem_batch_last_error",
             "vefem_stability_pattern", "vefem_stability_assemble",
             "vefem_frontal_create", "vefem_frontal_factor", "vefem_frontal_solve",
-            "vefem_frontal_destroy", "vefem_frontal_last_error"]
+            "vefem_frontal_destroy", "vefem_frontal_last_error", "vefem_frontal_solve_path"]
 VEFEM_ERR_SINGULAR = 6
 BATCH_CLASSES = 6
 
@@ -124,6 +124,7 @@ def load(path: str = LIB_PATH):
     L.vefem_frontal_destroy.restype = None
     L.vefem_frontal_last_error.argtypes = [P]
     L.vefem_frontal_last_error.restype = ctypes.c_char_p
+    L.vefem_frontal_solve_path.argtypes = [P]
     _lib = L
     return L
 
