@@ -92,6 +92,9 @@ def parse_args():
     ap.add_argument("--cont-arms", default="",
                     help="comma-separated arm names of the continuation comparison to run "
                          "(default: all)")
+    ap.add_argument("--krylov", type=int, default=10,
+                    help="GMRES iterations allowed per Newton-Krylov correction of the learned + "
+                         "mixed arm, in place of a new factorisation (0: chord steps only)")
     ap.add_argument("--newton-nel", type=int, default=40000,
                     help="mesh of the precision-form Newton comparison in the default line "
                          "(0 = skip it)")
@@ -330,7 +333,7 @@ def run_reference(args):
 
 def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=None,
                          secant: bool = True, step_log=None, ablations: bool = True,
-                         only=None, linear_solver: str = "auto"):
+                         only=None, linear_solver: str = "auto", krylov: int = 10):
     """Arclength continuation Wi 0.1 -> wi_end (Oldroyd-B, beta = 0.59, SQRT
     form) on the GPU assembly, arms from the same start: the plain FP64 path
     (FD64 Jacobian, the reference's tangent predictor), the same with a
@@ -362,7 +365,8 @@ def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=Non
     # the learned + mixed arm reuses factorisations across steps while chord
     # iterations contract (theta < 0.6) and cuts a failed step back (dS halved,
     # predicted again) before relaxing; the plain arm keeps the reference's rules
-    chord = dataclasses.replace(cfg, reuse="contraction", theta_max=0.6, cutbacks=4)
+    chord = dataclasses.replace(cfg, reuse="contraction", theta_max=0.6, cutbacks=4,
+                                krylov=krylov)
     arms, states = {}, {}
     runs = [("plain_fp64", "fd64", None, cfg), ("learned_fp32", "exact32", "learned", chord),
             ("learned_fp32_reference_reuse", "exact32", "learned", cfg),
@@ -396,7 +400,10 @@ def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=Non
             "predictor": {"learned": "learned POD/MLP", "secant": "secant", None: "tangent",
                           "ablate": "POD cubic extrapolation, network off"}[kind],
             "factorisation_reuse": arm_cfg.reuse if arm_cfg.reuse == "reference"
-            else f"contraction (theta_max {arm_cfg.theta_max}), {arm_cfg.cutbacks} step cutbacks",
+            else f"contraction (theta_max {arm_cfg.theta_max}), {arm_cfg.cutbacks} step cutbacks"
+            + (f", Newton-Krylov corrections (GMRES <= {arm_cfg.krylov} iterations, rtol "
+               f"{arm_cfg.krylov_rtol:g}) before a new factorisation" if arm_cfg.krylov else ""),
+            "gmres_iterations": cont.krylov_iterations, "gmres_misses": cont.krylov_failures,
             "wall_s": wall, "steps": len(recs), "steps_per_s": len(recs) / wall,
             "newton_iterations": sum(r.newton_iterations for r in recs),
             "factorisations": sum(r.factorisations for r in recs),
@@ -673,7 +680,7 @@ def run_vefem(args):
                 args.cont_nel, args.cont_wi, dev, secant=args.secant,
                 ablations=args.ablations,
                 only=[a for a in args.cont_arms.split(",") if a] or None,
-                linear_solver=args.linear_solver,
+                linear_solver=args.linear_solver, krylov=args.krylov,
                 step_log=(lambda m: print(m, file=sys.stderr, flush=True)) if args.cont_log else None)
             print(json.dumps({"continuation": out}))
         if dist:
@@ -868,7 +875,7 @@ def run_vefem(args):
     if world == 1 and args.cont_nel > 0:
         leg("continuation", lambda: continuation_compare(
             args.cont_nel, args.cont_wi, dev, secant=args.secant, ablations=args.ablations,
-            linear_solver=args.linear_solver))
+            linear_solver=args.linear_solver, krylov=args.krylov))
     if world == 1 and args.stab_nel > 0:
         leg("stability", lambda: stability_compare(args.stab_nel, max(3, args.steps // 4),
                                                    args.warmup, dev, cpu=not args.no_cpu_baseline))

@@ -123,6 +123,29 @@ def test_contraction_reuse_converges_on_the_same_branch_with_fewer_factorisation
     assert _branch_dev(out["reference"][1], out["contraction"][1]) < 1e-3
 
 
+def test_newton_krylov_corrections_stay_on_the_branch():
+    """Newton-Krylov corrections in place of factorisations (GMRES on the
+    Jacobian at the iterate, preconditioned by the older factorisation):
+    every point converged to ||R|| < 1e-10 on the branch of the chord-only
+    run, GMRES used, and no more factorisations than the chord-only run."""
+    from ve_flow_around_cylinder_fortran_gb300 import learned as LP
+    out = {}
+    for krylov in (0, 10):
+        cont, TL, EU = _driver(max_steps=400)
+        cont.cfg = C.ArclengthSettings(dArN=0.01, max_steps=400, lam_max=6.0,
+                                       reuse="contraction", theta_max=0.6, factor_cost=30.0,
+                                       krylov=krylov)
+        pred = LP.LearnedPredictor(n_modes=32, start=20, device="cpu", net=object(),
+                                   use_net=False)
+        recs, xs = cont.run(TL, EU, predictor=pred)
+        assert all(r.res_norm < 1e-10 for r in recs)
+        assert recs[-1].lam >= 6.0
+        out[krylov] = (sum(r.factorisations for r in recs), xs, cont.krylov_iterations)
+    assert out[10][2] > 0 and out[0][2] == 0
+    assert out[10][0] <= out[0][0]
+    assert _branch_dev(out[0][1], out[10][1]) < 1e-3
+
+
 def test_contraction_reuse_far_start_takes_newton_steps():
     """From the far initial state the chord policy takes full Newton steps
     while the correction is above MNR_eps, as the reference does, and

@@ -1,6 +1,7 @@
 """Host sparse LU stand-in (linsolve.py): nested-dissection order, solves, and
 the partial-pivoting fallback."""
 import numpy as np
+import pytest
 import scipy.sparse as sp
 import scipy.sparse.linalg as spla
 
@@ -73,3 +74,32 @@ def test_singular_diagonal_factor_falls_back(monkeypatch):
     assert lu.pivoted and lu.refactorisations == 1
     A = sp.csr_matrix((v, ci, rp), shape=(len(rp) - 1,) * 2)
     assert np.linalg.norm(A @ lu.solve(b) - b) <= 1e-10 * np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("kind", ["numpy", "torch"])
+def test_gmres_with_an_inexact_preconditioner(kind):
+    """Right-preconditioned GMRES with the LU of a perturbed matrix as the
+    preconditioner reaches the requested relative residual; with too few
+    iterations it reports the residual it reached."""
+    rng = np.random.default_rng(0)
+    n = 300
+    A = (sp.random(n, n, density=0.02, random_state=1) + 4.0 * sp.eye(n)).tocsr()
+    P_ = (A + 0.3 * sp.random(n, n, density=0.01, random_state=2)).tocsc()
+    lu = spla.splu(P_)
+    b = rng.standard_normal(n)
+    if kind == "numpy":
+        mv, pre, rhs, back = (lambda v: A @ v), lu.solve, b, (lambda x: x)
+    else:
+        torch = pytest.importorskip("torch")
+        At = torch.sparse_csr_tensor(torch.from_numpy(A.indptr).long(),
+                                     torch.from_numpy(A.indices).long(),
+                                     torch.from_numpy(A.data), size=A.shape)
+        mv = lambda v: At @ v                                        # noqa: E731
+        pre = lambda v: torch.from_numpy(lu.solve(v.numpy()))       # noqa: E731
+        rhs, back = torch.from_numpy(b), (lambda x: x.numpy())
+    x, its, rel = LS.gmres(mv, pre, rhs, 1e-10, 40)
+    x = back(x)
+    assert rel <= 1e-10 and its < 40
+    assert np.linalg.norm(A @ x - b) <= 1e-9 * np.linalg.norm(b)
+    _, its2, rel2 = LS.gmres(mv, pre, rhs, 1e-14, 2)
+    assert its2 == 2 and rel2 > 1e-14

@@ -87,6 +87,13 @@ class ArclengthSettings:
     # has taken ``cutback_factorisations`` factorisations without converging
     cutbacks: int = 0
     cutback_factorisations: int = 3
+    # Newton-Krylov corrections on an older factorisation ("contraction" reuse
+    # only): GMRES iterations allowed per correction (0: chord steps), its
+    # relative tolerance, and the iteration count beyond which the next
+    # iterate takes a new factorisation
+    krylov: int = 0
+    krylov_rtol: float = 1.0e-4
+    krylov_refactor: int = 8
 
 
 @dataclasses.dataclass
@@ -210,6 +217,9 @@ class ArclengthContinuation:
         self.t_iter = None
         self.t_fac = None
         self.reverted = 0        # chord steps undone because they did not contract
+        self.krylov_iterations = 0   # GMRES iterations of Newton-Krylov corrections
+        self.krylov_failures = 0     # corrections whose GMRES missed its tolerance
+        self.last_krylov_its = 0
 
     # state vector x = [TL in node-major order, lambda]
     def pack(self, TL, EU):
@@ -257,8 +267,19 @@ class ArclengthContinuation:
         iterate it started from; after a Newton step on a factorisation taken
         at its own starting point the Jacobian is assembled at the new iterate
         (the reference's 'MNR' -> 'NRP' switch).  With ``max_fac`` the solve
-        fails once it would take a factorisation beyond that many.  Returns
-        what _newton returns."""
+        fails once it would take a factorisation beyond that many.
+
+        With ``krylov`` > 0, where this policy would take a new factorisation
+        at an iterate that an older one could still serve (chord steps that
+        stopped contracting, mostly the stall of chord iterations close to
+        the solution), a Newton-Krylov step comes first: the Jacobian is
+        assembled at the iterate (cheap next to a factorisation) and J s = R
+        is solved by GMRES to ``krylov_rtol``, preconditioned by the older
+        factorisation; chord steps resume after it.  The factorisation is
+        taken (from the Jacobian just assembled) only when GMRES misses the
+        tolerance within ``krylov`` iterations, or at the next iterate after
+        a GMRES that needed more than ``krylov_refactor``.  Returns what
+        _newton returns."""
         cfg = self.cfg
         x = x0.copy()
         tm = self.timers
@@ -268,6 +289,7 @@ class ArclengthContinuation:
         prev_fresh = False       # the factorisation was taken at x_prev
         lu = self.solver if self.have_lu else None
         want = flag == "NRP" or lu is None
+        want_krylov = False
         it = nfac = 0
         while True:
             if cor_new < cfg.tol and res_norm < cfg.tol:
@@ -278,58 +300,81 @@ class ArclengthContinuation:
             self._update_inflow(float(EU[0]))
             if want and max_fac is not None and nfac >= max_fac:
                 return x, it, nfac, res_norm, lu, False
-            b, vals = self.dev(TL, EU, want)
+            krylov = want_krylov and not want and lu is not None
+            want_krylov = False
+            b, vals = self.dev(TL, EU, want or krylov)
             self.lrow(x, b, vals)
             res_norm = float(np.linalg.norm(b))
             t1 = time.perf_counter()
             if not np.isfinite(res_norm):
                 return x, it, nfac, res_norm, lu, False
+            s = None
+            if krylov:
+                s = self._krylov_solve(lu, vals, b)
+                if s is None:
+                    # GMRES did not converge: factorise the Jacobian just assembled
+                    if max_fac is not None and nfac >= max_fac:
+                        return x, it, nfac, res_norm, lu, False
+                    want = True
+            t_k = time.perf_counter()
             if want:
                 try:
                     lu = self.solver.factor(vals)
                 except RuntimeError:
                     self.failed_factorisations += 1
                     self.have_lu = False
-                    tm["factor"] += time.perf_counter() - t1
+                    tm["factor"] += time.perf_counter() - t_k
                     return x, it, nfac, res_norm, None, False
                 self.have_lu = True
                 nfac += 1
                 cor_old = None
             t2 = time.perf_counter()
-            try:
-                s = lu.solve(b)
-            except RuntimeError:
-                self.failed_factorisations += 1
-                self.have_lu = False
-                return x, it, nfac, res_norm, None, False
+            if s is None:
+                try:
+                    s = lu.solve(b)
+                except RuntimeError:     # its pivoted re-factorisation was singular
+                    self.failed_factorisations += 1
+                    self.have_lu = False
+                    return x, it, nfac, res_norm, None, False
             t3 = time.perf_counter()
             tm["assembly"] += t1 - t0
-            tm["factor"] += t2 - t1
-            tm["solve"] += t3 - t2
+            tm["factor"] += t2 - t_k
+            tm["solve"] += (t3 - t2) + (t_k - t1)
             if want:
-                c = (t1 - t0) + (t2 - t1)
+                c = (t1 - t0) + (t2 - t_k)
                 self.t_fac = c if self.t_fac is None else 0.5 * (self.t_fac + c)
             else:
-                c = (t1 - t0) + (t3 - t2)
+                c = (t1 - t0) + (t3 - t2) + (t_k - t1)
                 self.t_iter = c if self.t_iter is None else 0.5 * (self.t_iter + c)
             cor_new = float(np.linalg.norm(s))
             if it == 1:
                 self.cor0 = cor_new
             if self.log:
-                self.log(f"   {it:3d}. {'NRP' if want else 'MNR'}: RES_NORM = {res_norm:.4e}, "
+                mode = "NRP" if want else ("NK" if krylov else "MNR")
+                self.log(f"   {it:3d}. {mode}: RES_NORM = {res_norm:.4e}, "
                          f"COR_NORM = {cor_new:.4e}")
             if cor_new != cor_new or cor_new > NW.COR_NORM_DIV or it > max_iter:
                 return x, it, nfac, res_norm, lu, False
             fresh = want
             want = False
+            # a Newton-Krylov step in place of the factorisation the rules
+            # below ask for (not after a fresh factorisation, nor right after
+            # a Newton-Krylov step that needed many GMRES iterations)
+            use_krylov = cfg.krylov > 0 and not fresh and \
+                not (krylov and self.last_krylov_its > cfg.krylov_refactor)
             if cor_old is not None and cor_new >= cfg.tol:
                 theta = cor_new / cor_old
                 if theta >= 1.0 and not prev_fresh:
                     # a stale factorisation that does not contract: undo the
-                    # chord step, refactorise where it started
+                    # chord step, refactorise (or take a Newton-Krylov step)
+                    # where it started
                     self.reverted += 1
                     x = x_prev
-                    cor_new, want = cor_old, True
+                    cor_new = cor_old
+                    if use_krylov and not krylov:
+                        want_krylov = True
+                    else:
+                        want = True
                     continue
                 if theta >= cfg.theta_max:
                     want = True
@@ -340,9 +385,50 @@ class ArclengthContinuation:
                 # far from the solution: full Newton steps, as the reference
                 # stays in 'NRP' until the correction drops below MNR_eps
                 want = True
+            if krylov and self.last_krylov_its > cfg.krylov_refactor:
+                want = True
+            elif want and use_krylov:
+                want, want_krylov = False, True
             cor_old = cor_new
             x_prev, prev_fresh = x, fresh
             x = x - xF * s
+
+    def _krylov_solve(self, lu, vals, b):
+        """GMRES on J s = b with the Jacobian values ``vals`` (device tensor or
+        host array, lambda and Dirichlet rows applied) and the factorisation
+        ``lu`` as right preconditioner; the correction as a host array, or
+        None when GMRES did not reach ``krylov_rtol``."""
+        cfg = self.cfg
+        if isinstance(vals, np.ndarray):
+            import scipy.sparse as sp
+            J = sp.csr_matrix((vals, self.lrow.colind, self.lrow.rowptr), shape=(self.N, self.N))
+            rhs = np.asarray(b, dtype=np.float64)
+            pre = getattr(lu, "precondition", lu.solve)
+            s, its, rel = LS.gmres(lambda v: J @ v, pre, rhs, cfg.krylov_rtol, cfg.krylov)
+        else:
+            import warnings
+
+            import torch
+            dev = vals.device
+            if getattr(self, "_csr_dev", None) != dev:
+                self._crow = torch.from_numpy(self.lrow.rowptr.astype(np.int64)).to(dev)
+                self._col = torch.from_numpy(self.lrow.colind.astype(np.int64)).to(dev)
+                self._csr_dev = dev
+            with warnings.catch_warnings():
+                warnings.simplefilter("ignore")
+                J = torch.sparse_csr_tensor(self._crow, self._col, vals.to(torch.float64),
+                                            size=(self.N, self.N), check_invariants=False)
+            rhs = torch.from_numpy(np.ascontiguousarray(b, dtype=np.float64)).to(dev)
+            pre = lu.precondition if hasattr(lu, "precondition") else \
+                (lambda v: torch.from_numpy(lu.solve(v.cpu().numpy())).to(dev))
+            s, its, rel = LS.gmres(lambda v: J @ v, pre, rhs, cfg.krylov_rtol, cfg.krylov)
+            s = s.cpu().numpy()
+        self.last_krylov_its = its
+        self.krylov_iterations += its
+        if not (rel <= cfg.krylov_rtol) or not np.all(np.isfinite(s)):
+            self.krylov_failures += 1
+            return None
+        return s
 
     def _newton(self, x0: np.ndarray, xF: float = 1.0, max_iter: int = NW.NITER,
                 flag: str = "NRP", max_fac: int | None = None):

@@ -405,6 +405,14 @@ class FrontalLU:
             x[self.idxP[q]] = xP
         return x
 
+    def precondition(self, b):
+        """The last factorisation's solve as a preconditioner: the sweeps only,
+        without the residual check (a device tensor in, a device tensor out;
+        a host array goes through solve)."""
+        if self._host is not None or isinstance(b, np.ndarray):
+            return self.solve(b)
+        return self._sweep(b.to(device=self.dev, dtype=self.torch.float64))
+
     def solve(self, b):
         """Solve with the last factorisation; ``b`` a host array (returns a host
         array) or a device tensor (returns a device tensor).

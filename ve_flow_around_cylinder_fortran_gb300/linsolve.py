@@ -103,6 +103,11 @@ class SparseLU:
         self.pivoted = True
         self.refactorisations += 1
 
+    def precondition(self, b: np.ndarray) -> np.ndarray:
+        """A solve with the last factorisation as a preconditioner (the same
+        as solve)."""
+        return self.solve(b)
+
     def solve(self, b: np.ndarray) -> np.ndarray:
         if self.perm is None:
             return self.lu.solve(b)
@@ -117,6 +122,60 @@ class SparseLU:
         x = np.empty_like(xp)
         x[self.perm] = xp
         return x
+
+
+def gmres(matvec, precond, b, rtol: float, maxiter: int):
+    """Right-preconditioned GMRES for A x = b (Saad, "Iterative Methods for
+    Sparse Linear Systems", 2nd ed., Algorithm 9.5): the Arnoldi basis of
+    A M^-1 by classical Gram-Schmidt applied twice, the small least-squares
+    problem on the host.  ``b`` is a numpy array or a torch tensor (any
+    device); ``matvec`` and ``precond`` take and return the same kind.
+    Stops once the residual estimate is at most rtol |b| or after
+    ``maxiter`` iterations.  Returns (x, iterations, relative residual
+    estimate)."""
+    is_np = isinstance(b, np.ndarray)
+    if is_np:
+        xp = np
+        nrm = lambda v: float(np.linalg.norm(v))               # noqa: E731
+        basis = np.empty((maxiter + 1, b.shape[0]), dtype=b.dtype)
+        to_host = lambda c: c                                   # noqa: E731
+        to_dev = lambda c: c                                    # noqa: E731
+    else:
+        import torch as xp
+        nrm = lambda v: float(xp.linalg.vector_norm(v))         # noqa: E731
+        basis = xp.empty((maxiter + 1, b.shape[0]), dtype=b.dtype, device=b.device)
+        to_host = lambda c: c.cpu().numpy()                     # noqa: E731
+        to_dev = lambda c: xp.from_numpy(c).to(device=b.device, dtype=b.dtype)  # noqa: E731
+    beta = nrm(b)
+    if beta == 0.0 or not np.isfinite(beta):
+        return b * 0.0, 0, 0.0 if beta == 0.0 else float("nan")
+    basis[0] = b / beta
+    Z = []
+    H = np.zeros((maxiter + 1, maxiter))
+    for j in range(maxiter):
+        z = precond(basis[j])
+        Z.append(z)
+        w = matvec(z)
+        V = basis[:j + 1]
+        h = np.zeros(j + 1)
+        for _ in range(2):
+            c = to_host(V @ w)
+            w = w - V.T @ to_dev(c)
+            h += c
+        hn = nrm(w)
+        H[:j + 1, j] = h
+        H[j + 1, j] = hn
+        e1 = np.zeros(j + 2)
+        e1[0] = beta
+        y = np.linalg.lstsq(H[:j + 2, :j + 1], e1, rcond=None)[0]
+        res = float(np.linalg.norm(H[:j + 2, :j + 1] @ y - e1))
+        if res <= rtol * beta or not hn > 0.0 or j == maxiter - 1 or not np.isfinite(res):
+            x = Z[0] * float(y[0])
+            for i in range(1, j + 1):
+                x = x + Z[i] * float(y[i])
+            return x, j + 1, res / beta
+        basis[j + 1] = w / hn
+    raise AssertionError("unreachable")
 
 
 def make_solver(kind, rowptr: np.ndarray, colind: np.ndarray, mesh=None, **kw):

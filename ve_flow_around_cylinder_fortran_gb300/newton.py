@@ -230,14 +230,34 @@ def emergency_solve(newton, TL, EU, log=None, **kw):
     return res
 
 
+def extrapolate(wis_done, TLs, wi: float) -> np.ndarray:
+    """Start of the next natural-continuation point: the Lagrange polynomial
+    in Wi through the last (up to three) converged states, evaluated at
+    ``wi`` -- the reference's transient predictor (updateSolutionTransient,
+    Continuation_Transient_mod.F90:188-243: TLp = Lb TLb + Lo TLo + L TL)
+    with Wi in place of time."""
+    w = list(wis_done[-3:])
+    X = list(TLs[-3:])
+    out = np.zeros_like(X[-1])
+    for i in range(len(w)):
+        c = 1.0
+        for j in range(len(w)):
+            if j != i:
+                c *= (wi - w[j]) / (w[i] - w[j])
+        out += c * X[i]
+    return out
+
+
 def natural_continuation(asm, mesh, phys: S.Physics, wis, jacobian: str = "fd64",
                          tol: float = 1.0e-10, outlet_edges: bool = True, TL=None, log=None,
-                         linear_solver="superlu"):
-    """Solve at each Weissenberg number of ``wis`` in turn, each from the
-    previous solution (the inflow Dirichlet data follow Wi).  Returns the list
-    of NewtonResult."""
+                         linear_solver="superlu", predictor: bool = True):
+    """Solve at each Weissenberg number of ``wis`` in turn (the inflow
+    Dirichlet data follow Wi), each from the previous solution or, with
+    ``predictor``, from the extrapolation through the last converged
+    solutions (``extrapolate``).  Returns the list of NewtonResult."""
     out = []
     EU = np.ones(phys.nex)
+    done_w, done_TL = [], []
     # one solver for all points (the frontal LU's symbolic phase is per mesh)
     solver = LS.make_solver(linear_solver, asm.rowptr, asm.colind, mesh)
     for wi in wis:
@@ -246,6 +266,8 @@ def natural_continuation(asm, mesh, phys: S.Physics, wis, jacobian: str = "fd64"
         rows, values = boundary_conditions(mesh, p)
         if TL is None:
             TL, EU = initial_state(mesh, p)
+        elif predictor and len(done_w) >= 2:
+            TL = extrapolate(done_w, done_TL, wi)
         TL = np.ascontiguousarray(TL)
         nr = NewtonRaphson(DeviceAssembly(asm, rows, values, jacobian, outlet_edges),
                            asm.rowptr, asm.colind, p.nex, mesh, linear_solver=solver)
@@ -254,6 +276,8 @@ def natural_continuation(asm, mesh, phys: S.Physics, wis, jacobian: str = "fd64"
             raise RuntimeError(f"Newton did not converge at Wi = {wi}")
         out.append(res)
         TL, EU = res.TL, res.EU
+        done_w.append(wi)
+        done_TL.append(res.TL)
     return out
 
 
