@@ -92,7 +92,7 @@ def parse_args():
     ap.add_argument("--cont-arms", default="",
                     help="comma-separated arm names of the continuation comparison to run "
                          "(default: all)")
-    ap.add_argument("--krylov", type=int, default=10,
+    ap.add_argument("--krylov", type=int, default=0,
                     help="GMRES iterations allowed per Newton-Krylov correction of the learned + "
                          "mixed arm, in place of a new factorisation (0: chord steps only)")
     ap.add_argument("--newton-nel", type=int, default=40000,
@@ -333,7 +333,7 @@ def run_reference(args):
 
 def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=None,
                          secant: bool = True, step_log=None, ablations: bool = True,
-                         only=None, linear_solver: str = "auto", krylov: int = 10):
+                         only=None, linear_solver: str = "auto", krylov: int = 0):
     """Arclength continuation Wi 0.1 -> wi_end (Oldroyd-B, beta = 0.59, SQRT
     form) on the GPU assembly, arms from the same start: the plain FP64 path
     (FD64 Jacobian, the reference's tangent predictor), the same with a
@@ -483,20 +483,30 @@ def newton_precision_compare(nel: int, device: int = 0, wis=(0.1, 0.2, 0.3, 0.4,
     runs, final = {}, {}
     for jac in ("fd64", "exact32"):
         t0 = time.perf_counter()
+        # a point whose Newton iteration diverges ends the run (no emergency
+        # restarts: relaxed Newton at this size takes minutes per attempt);
+        # the points before it are reported
         res = NW.natural_continuation(asm, mesh, phys, list(wis), jacobian=jac, tol=1e-10,
-                                      linear_solver=solver)
+                                      linear_solver=solver, max_restarts=0,
+                                      stop_on_failure=True)
         wall = time.perf_counter() - t0
         runs[jac] = {
             "wall_s": wall,
+            "reached_wi": wis[len(res) - 1] if res else None,
+            "stopped_at_wi": wis[len(res)] if len(res) < len(wis) else None,
             "solves": [{"wi": wi, "iterations": r.iterations,
                         "factorisations": sum(h["flag"] == "NRP" for h in r.history),
                         "final_res_norm": r.history[-1]["res_norm"],
                         "assembly_s": r.assembly_s, "factor_and_solve_s": r.solve_s}
                        for wi, r in zip(wis, res)],
         }
-        final[jac] = res[-1].TL
+        final[jac] = [r.TL for r in res]
     asm.close()
-    d = final["exact32"] - final["fd64"]
+    common = min(len(final["fd64"]), len(final["exact32"]))
+    if common == 0:
+        raise RuntimeError("no Weissenberg number converged in both runs")
+    ref = final["fd64"][common - 1]
+    d = final["exact32"][common - 1] - ref
     return {
         "workload": f"Newton solves by natural continuation Wi = {', '.join(str(w) for w in wis)}, "
                     f"Giesekus alpha=0.1, beta=0.59, SQRT form, {mesh.nel} Q2 quads "
@@ -504,8 +514,9 @@ def newton_precision_compare(nel: int, device: int = 0, wis=(0.1, 0.2, 0.3, 0.4,
                     f"linear solver: {_solver_desc(solver)}",
         "linear_solver": type(solver).__name__, "solver_setup_s": t_sym,
         "fd64": runs["fd64"], "fp32_jacobian": runs["exact32"],
-        "solution_rel_err_2norm": float(np.linalg.norm(d) / np.linalg.norm(final["fd64"])),
-        "solution_rel_err_maxnorm": float(np.max(np.abs(d)) / np.max(np.abs(final["fd64"]))),
+        "solution_error_at_wi": wis[common - 1],
+        "solution_rel_err_2norm": float(np.linalg.norm(d) / np.linalg.norm(ref)),
+        "solution_rel_err_maxnorm": float(np.max(np.abs(d)) / np.max(np.abs(ref))),
     }
 
 
@@ -867,9 +878,11 @@ def run_vefem(args):
         if "fp32_jacobian" in npr:
             line["fp32_jacobian"]["newton"] = {
                 "workload": npr["workload"],
+                "reached_wi": npr["fp32_jacobian"]["reached_wi"],
                 "iterations": [x["iterations"] for x in npr["fp32_jacobian"]["solves"]],
                 "factorisations": [x["factorisations"] for x in npr["fp32_jacobian"]["solves"]],
                 "fp64_iterations": [x["iterations"] for x in npr["fd64"]["solves"]],
+                "solution_error_at_wi": npr["solution_error_at_wi"],
                 "solution_rel_err_2norm": npr["solution_rel_err_2norm"],
                 "solution_rel_err_maxnorm": npr["solution_rel_err_maxnorm"]}
     if world == 1 and args.cont_nel > 0:

@@ -231,3 +231,38 @@ def test_garbage_predictions_are_rejected_by_the_residual_judge():
     assert len(r0) == len(r1)
     for a, b in zip(x0, x1):
         assert np.array_equal(a, b)
+
+
+def test_natural_continuation_extrapolation_is_lagrange_in_wi():
+    """The start of the next natural-continuation point: exact for states
+    that are polynomials of degree <= 2 in Wi, from the last three points."""
+    rng = np.random.default_rng(0)
+    a, b, c = (rng.standard_normal((6, 5)) for _ in range(3))
+    f = lambda w: a + b * w + c * w * w                           # noqa: E731
+    ws = [0.1, 0.2, 0.3, 0.4]
+    X = [f(w) for w in ws]
+    assert np.allclose(N.extrapolate(ws, X, 0.55), f(0.55), rtol=0, atol=1e-12)
+    # two points: the secant
+    assert np.allclose(N.extrapolate(ws[:2], X[:2], 0.3), 2 * X[1] - X[0], atol=1e-12)
+
+
+def test_emergency_restarts_are_bounded():
+    """emergencyNewtonRaphson halves the relaxation until xF < 1e-2; with
+    max_restarts the caller bounds the number of restarts."""
+    class Diverging:
+        def __init__(self):
+            self.calls = []
+
+        def solve(self, TL, EU, xF=1.0, log=None, **kw):
+            self.calls.append(xF)
+            return N.NewtonResult(TL, EU, False, 1, [], 0.0, 0.0)
+
+    nr = Diverging()
+    res = N.emergency_solve(nr, np.zeros((6, 2)), np.zeros(0))
+    assert not res.converged and nr.calls == [1.0, 0.5, 0.25, 0.125, 0.0625, 0.03125, 0.015625]
+    nr = Diverging()
+    N.emergency_solve(nr, np.zeros((6, 2)), np.zeros(0), max_restarts=1)
+    assert nr.calls == [1.0, 0.5]
+    nr = Diverging()
+    N.emergency_solve(nr, np.zeros((6, 2)), np.zeros(0), max_restarts=0)
+    assert nr.calls == [1.0]

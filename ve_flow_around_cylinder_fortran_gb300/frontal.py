@@ -361,10 +361,18 @@ class FrontalLU:
             self._to_host()
         return self
 
+    HOST_MAX_UNKNOWNS = 300_000
+
     def _to_host(self):
         """Factorise on the host instead (a zero pivot, or a solve that stays
-        inaccurate after refinement)."""
+        inaccurate after refinement).  Above HOST_MAX_UNKNOWNS the host LU
+        runs out of memory (SuperLU's 32-bit indices overflow around a
+        million unknowns), so the factorisation fails with RuntimeError at
+        once, which the Newton drivers treat as a failed solve."""
         from . import linsolve as LS
+        if self.N > self.HOST_MAX_UNKNOWNS:
+            raise RuntimeError(f"no pivot-stable factorisation on the device and {self.N} "
+                               f"unknowns are beyond the host fallback")
         self.fallbacks += 1
         self._host = LS.SparseLU(self.rowptr, self.colind, self.mesh, neq=self.neq)
         self._host.factor(self.vals.cpu().numpy())

@@ -213,16 +213,19 @@ class DeviceAssembly:
         return b, self.vals.cpu().numpy().astype(np.float64)
 
 
-def emergency_solve(newton, TL, EU, log=None, **kw):
+def emergency_solve(newton, TL, EU, log=None, max_restarts=None, **kw):
     """emergencyNewtonRaphson (Newton_Raphson_mod.F90:533-584): on divergence
     restart from the same state with the relaxation factor halved and
-    50 x Niter iterations allowed, until xF < 1e-2."""
+    50 x Niter iterations allowed, until xF < 1e-2 (or after ``max_restarts``
+    restarts, when given)."""
     xF = kw.pop("xF", 1.0)
     res = newton.solve(TL, EU, xF=xF, log=log, **kw)
+    restarts = 0
     while not res.converged:
         xF = xF / 2.0
-        if xF < 1.0e-2:
+        if xF < 1.0e-2 or (max_restarts is not None and restarts >= max_restarts):
             return res
+        restarts += 1
         if log:
             log(f"restarting with relaxation xF = {xF}")
         kw["max_iter"] = 50 * NITER
@@ -250,11 +253,15 @@ def extrapolate(wis_done, TLs, wi: float) -> np.ndarray:
 
 def natural_continuation(asm, mesh, phys: S.Physics, wis, jacobian: str = "fd64",
                          tol: float = 1.0e-10, outlet_edges: bool = True, TL=None, log=None,
-                         linear_solver="superlu", predictor: bool = True):
+                         linear_solver="superlu", predictor: bool = True,
+                         max_restarts=None, stop_on_failure: bool = False):
     """Solve at each Weissenberg number of ``wis`` in turn (the inflow
     Dirichlet data follow Wi), each from the previous solution or, with
     ``predictor``, from the extrapolation through the last converged
-    solutions (``extrapolate``).  Returns the list of NewtonResult."""
+    solutions (``extrapolate``).  ``max_restarts`` bounds the emergency
+    restarts per point; a point that does not converge raises, or with
+    ``stop_on_failure`` ends the run.  Returns the list of NewtonResult of
+    the converged points."""
     out = []
     EU = np.ones(phys.nex)
     done_w, done_TL = [], []
@@ -271,8 +278,15 @@ def natural_continuation(asm, mesh, phys: S.Physics, wis, jacobian: str = "fd64"
         TL = np.ascontiguousarray(TL)
         nr = NewtonRaphson(DeviceAssembly(asm, rows, values, jacobian, outlet_edges),
                            asm.rowptr, asm.colind, p.nex, mesh, linear_solver=solver)
-        res = emergency_solve(nr, TL, EU, log=log, tol=tol)
+        try:
+            res = emergency_solve(nr, TL, EU, log=log, tol=tol, max_restarts=max_restarts)
+        except (RuntimeError, FloatingPointError):
+            if not stop_on_failure:
+                raise
+            break
         if not res.converged:
+            if stop_on_failure:
+                break
             raise RuntimeError(f"Newton did not converge at Wi = {wi}")
         out.append(res)
         TL, EU = res.TL, res.EU
