@@ -110,7 +110,8 @@ def parse_args():
                     help="instances of the batched-form measurement (0 = skip it)")
     ap.add_argument("--stab-nel", type=int, default=20000,
                     help="mesh of the linear-stability measurement (0 = skip it)")
-    ap.add_argument("--only", choices=["fd64", "residual", "exact64", "exact32", "stability"],
+    ap.add_argument("--only", choices=["fd64", "residual", "exact64", "exact32", "stability",
+                                       "frontal"],
                     default=None,
                     help="time one assembly form alone on the --nel workload (profiling case)")
     return ap.parse_args()
@@ -363,10 +364,12 @@ def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=Non
     solver_name = type(solver).__name__
     cfg = C.ArclengthSettings(dArN=0.01, lam_max=wi_end / phys.Wi0, max_steps=2000)
     # the learned + mixed arm reuses factorisations across steps while chord
-    # iterations contract (theta < 0.6) and cuts a failed step back (dS halved,
-    # predicted again) before relaxing; the plain arm keeps the reference's rules
+    # iterations contract (theta < 0.6), cuts a failed step back (dS halved,
+    # predicted again) before relaxing, and checks its solves to 1e-8 relative
+    # residual (an inexact Newton by design); the plain arm keeps the
+    # reference's rules and the solver's 1e-10 check
     chord = dataclasses.replace(cfg, reuse="contraction", theta_max=0.6, cutbacks=4,
-                                krylov=krylov)
+                                krylov=krylov, solve_check_tol=1.0e-8)
     arms, states = {}, {}
     runs = [("plain_fp64", "fd64", None, cfg), ("learned_fp32", "exact32", "learned", chord),
             ("learned_fp32_reference_reuse", "exact32", "learned", cfg),
@@ -399,6 +402,8 @@ def continuation_compare(nel: int, wi_end: float = 1.0, device: int = 0, log=Non
             "jacobian": jac,
             "predictor": {"learned": "learned POD/MLP", "secant": "secant", None: "tangent",
                           "ablate": "POD cubic extrapolation, network off"}[kind],
+            "solve_check_rel_residual": arm_cfg.solve_check_tol
+            if arm_cfg.solve_check_tol is not None else getattr(solver, "check_tol", None),
             "factorisation_reuse": arm_cfg.reuse if arm_cfg.reuse == "reference"
             else f"contraction (theta_max {arm_cfg.theta_max}), {arm_cfg.cutbacks} step cutbacks"
             + (f", Newton-Krylov corrections (GMRES <= {arm_cfg.krylov} iterations, rtol "
@@ -503,20 +508,21 @@ def newton_precision_compare(nel: int, device: int = 0, wis=(0.1, 0.2, 0.3, 0.4,
         final[jac] = [r.TL for r in res]
     asm.close()
     common = min(len(final["fd64"]), len(final["exact32"]))
-    if common == 0:
-        raise RuntimeError("no Weissenberg number converged in both runs")
-    ref = final["fd64"][common - 1]
-    d = final["exact32"][common - 1] - ref
+    err = {"solution_error_at_wi": None, "solution_rel_err_2norm": None,
+           "solution_rel_err_maxnorm": None}
+    if common:
+        ref = final["fd64"][common - 1]
+        d = final["exact32"][common - 1] - ref
+        err = {"solution_error_at_wi": wis[common - 1],
+               "solution_rel_err_2norm": float(np.linalg.norm(d) / np.linalg.norm(ref)),
+               "solution_rel_err_maxnorm": float(np.max(np.abs(d)) / np.max(np.abs(ref)))}
     return {
         "workload": f"Newton solves by natural continuation Wi = {', '.join(str(w) for w in wis)}, "
                     f"Giesekus alpha=0.1, beta=0.59, SQRT form, {mesh.nel} Q2 quads "
                     f"({len(rowptr) - 1} unknowns), outlet edges, Dirichlet rows on the device; "
                     f"linear solver: {_solver_desc(solver)}",
         "linear_solver": type(solver).__name__, "solver_setup_s": t_sym,
-        "fd64": runs["fd64"], "fp32_jacobian": runs["exact32"],
-        "solution_error_at_wi": wis[common - 1],
-        "solution_rel_err_2norm": float(np.linalg.norm(d) / np.linalg.norm(ref)),
-        "solution_rel_err_maxnorm": float(np.max(np.abs(d)) / np.max(np.abs(ref))),
+        "fd64": runs["fd64"], "fp32_jacobian": runs["exact32"], **err,
     }
 
 
@@ -618,6 +624,65 @@ def run_only(args, asm, mesh, TL, EU, cfg, dev):
     return 0
 
 
+def frontal_solve_timing(nel: int, steps: int, warmup: int, device: int = 0):
+    """The continuation's linear solver alone (the profiling case): the GPU
+    panel-frontal LU of the bordered FD64 Jacobian of a perturbed fully
+    developed Oldroyd-B state (Wi = 0.5, SQRT form, arclength row), one
+    factorisation and ``steps`` solves timed with CUDA events on the
+    current stream, the solve checked against the CSR matrix."""
+    import torch
+    from ve_flow_around_cylinder_fortran_gb300 import continuation as C
+    from ve_flow_around_cylinder_fortran_gb300 import frontal as FR
+    from ve_flow_around_cylinder_fortran_gb300 import newton as NW
+    mesh = M.build_cylinder_mesh(nel)
+    phys = S.oldroyd_b(0.5, 0.59, "SQRT", nex=1)
+    rp, ci = P.build_pattern(mesh.element_nodes(), mesh.nnodes, 1)
+    asm = V.BulkAssembler(mesh, phys, rp, ci, outlet_edges=True, device=device)
+    rows, values = NW.boundary_conditions(mesh, phys)
+    TL, EU = NW.initial_state(mesh, phys)
+    TLs, _ = S.seeded_state(mesh.xyz, phys, 0)
+    TL = TL + 0.01 * (TLs - TL)
+    dev = NW.DeviceAssembly(asm, rows, values, "fd64", True)
+    b, vals = dev(TL, EU, True)
+    asm.close()
+    lrow = C.LambdaRow(rp, ci)
+    x = np.concatenate([TL.T.reshape(-1), EU])
+    t = np.random.default_rng(0).standard_normal(len(x))
+    lrow.mode, lrow.t, lrow.x_o, lrow.dS = "arclength", t / np.linalg.norm(t), x * 0.99, 0.1
+    lrow(x, b, vals)
+    lu = FR.FrontalLU(rp, ci, mesh)
+    d = torch.device(f"cuda:{device}")
+    dv = torch.from_numpy(vals).to(d)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lu.factor(dv)
+    torch.cuda.synchronize()
+    t_fac = time.perf_counter() - t0
+    bt = torch.from_numpy(b).to(d)
+    xs = lu._sweep(bt)
+    rel = float(torch.linalg.vector_norm(bt - lu.A @ xs) / torch.linalg.vector_norm(bt))
+    for _ in range(warmup):
+        lu._sweep(bt)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record()
+    for _ in range(steps):
+        xr = lu._sweep(bt)
+    ev1.record()
+    torch.cuda.synchronize()
+    out = {"workload": f"bordered FD64 Jacobian, {mesh.nel} Q2 quads ({len(rp) - 1} unknowns), "
+                       f"Oldroyd-B Wi=0.5 SQRT, perturbed fully developed state; "
+                       f"{_solver_desc(lu)}",
+           "factor_s": t_fac, "factor_mode": lu.mode, "min_relative_pivot": lu.min_pivot,
+           "solve_ms": ev0.elapsed_time(ev1) / steps, "launches_per_solve": 2 * lu.npan + 2,
+           "solve_path": {1: "programmatic dependent launch", 2: "plain stream order"}.get(
+               lu.solve_path, None),
+           "solve_rel_residual": rel, "reproducible": bool(torch.equal(xs, xr))}
+    lu.close()
+    return out
+
+
 def stability_compare(nel: int, steps: int, warmup: int, device: int = 0, cpu: bool = True):
     """Linear stability (Oldroyd-B, beta = 0.59, Wi = 0.7, T form): A(k) for
     16 spanwise wavenumbers uniform in [0, 4] and B, 10 unknowns per node, on
@@ -674,6 +739,11 @@ def run_vefem(args):
     dev = local
     torch.cuda.set_device(dev)
     B.build()
+    if args.only == "frontal":
+        if rank == 0:
+            print(json.dumps({"only": "frontal", "frontal": frontal_solve_timing(
+                args.nel, args.steps, args.warmup, dev)}))
+        return 0
     if args.only == "stability":
         if rank == 0:
             print(json.dumps({"only": "stability",

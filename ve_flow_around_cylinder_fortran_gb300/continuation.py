@@ -94,6 +94,11 @@ class ArclengthSettings:
     krylov: int = 0
     krylov_rtol: float = 1.0e-4
     krylov_refactor: int = 8
+    # relative residual a linear solve is checked (and refined) against
+    # during this run; None keeps the solver's own (1e-10 for the GPU
+    # frontal LU).  An inexact Newton (stale factorisations, FP32 Jacobian)
+    # needs no 1e-10 solves: its corrections are approximate by design
+    solve_check_tol: float | None = None
 
 
 @dataclasses.dataclass
@@ -501,6 +506,16 @@ class ArclengthContinuation:
     def run(self, TL0: np.ndarray, EU0: np.ndarray, predictor=None):
         """Continue from (TL0, EU0) until lambda >= lam_max; returns the step
         records and the converged states."""
+        saved = getattr(self.solver, "check_tol", None)
+        if self.cfg.solve_check_tol is not None and saved is not None:
+            self.solver.check_tol = self.cfg.solve_check_tol
+        try:
+            return self._run(TL0, EU0, predictor)
+        finally:
+            if saved is not None:
+                self.solver.check_tol = saved
+
+    def _run(self, TL0: np.ndarray, EU0: np.ndarray, predictor=None):
         cfg = self.cfg
         x_p = self.pack(TL0, EU0)
         x_p[-1] = cfg.LN0
