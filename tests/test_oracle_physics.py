@@ -228,3 +228,36 @@ def test_gauss_tables_partition_of_unity():
     assert abs(w.sum() - 4.0) < 1e-15
     # the 0 + 1e-8 "centre" point: basis of corner node 1 is tiny but not zero there
     assert 0 < abs(bfn[0, 0]) < 1e-8
+
+
+def test_fd_jacobian_nan_at_exact_parallel_flow():
+    """A quirk of the reference algorithm the restatement keeps: on element
+    20478 of the 40,000-quad mesh at the fully developed Giesekus start
+    (tests/golden/fd_nan_element.json, exact bits) the residual is finite but
+    perturbing S12 at local nodes 1 and 3 by the FD step 1e-8 makes the
+    residual NaN.  The SQRT form's LSCE coefficient holds the magnitude
+    sqrt(0.5 Con_EQ : Con_EQ^T) with doubleDotProduct(A, B) = sum A_ij B_ji
+    (Tools_mod.F90:262-278, Element_Calculations_mod.F90:762-768); Con_EQ
+    vanishes for parallel flow, and after the perturbation the off-diagonal
+    product of opposite signs dominates the sum, so the square root is of a
+    negative number (here: tlsce NaN at the perturbed state)."""
+    import json
+    import os
+    d = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "fd_nan_element.json")))
+    xyz = np.array([[float.fromhex(v) for v in r] for r in d["xyz"]])
+    TL = np.array([[float.fromhex(v) for v in r] for r in d["TL"]])
+    conn = np.arange(1, 10, dtype=np.int32).reshape(9, 1)
+    phys = S.giesekus(0.1, 0.1, 0.59, "SQRT", nex=0)
+    EU = np.zeros(0)
+    res, jac, _ = O.element_outputs(phys, conn, xyz, TL, EU)
+    assert np.all(np.isfinite(res))
+    bad = np.argwhere(~np.isfinite(jac[0]))
+    assert len(bad) == 90
+    # the perturbed unknown (inod, ieq): S12 (field 4) of local nodes 1 and 3
+    assert set(map(tuple, bad[:, :2])) == {(1, 4), (3, 4)}
+    assert np.all(np.isfinite(O.gp_probe(phys, conn, xyz, TL, EU, 0)))
+    TLp = TL.copy()
+    TLp[4, 1] = TLp[4, 1] + 1.0e-8
+    probe = O.gp_probe(phys, conn, xyz, TLp, EU, 0)
+    assert np.all(np.isfinite(probe[:, 3:6]))          # Con_EQ 11/12/22 themselves finite
+    assert np.any(np.isnan(probe[:, 8]))                # tlsce
