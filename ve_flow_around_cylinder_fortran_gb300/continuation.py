@@ -94,6 +94,9 @@ class ArclengthSettings:
     krylov: int = 0
     krylov_rtol: float = 1.0e-4
     krylov_refactor: int = 8
+    # with krylov > 0: the arclength tangent from the Jacobian at the converged
+    # point by GMRES (an older factorisation tilts the arclength plane)
+    krylov_tangent: bool = True
     # relative residual a linear solve is checked (and refined) against
     # during this run; None keeps the solver's own (1e-10 for the GPU
     # frontal LU).  An inexact Newton (stale factorisations, FP32 Jacobian)
@@ -597,7 +600,17 @@ class ArclengthContinuation:
                 e_l = np.zeros(self.N)
                 e_l[-1] = 1.0
                 ts = time.perf_counter()
-                tv = lu.solve(e_l)
+                tv = None
+                if cfg.krylov > 0 and cfg.krylov_tangent:
+                    # the tangent of the Jacobian at the converged point, by
+                    # GMRES preconditioned with the (possibly older) factorisation
+                    TLc, EUc = self.unpack(x)
+                    self._update_inflow(float(EUc[0]))
+                    _, vals_c = self.dev(TLc, EUc, True)
+                    self.lrow(x, np.zeros(self.N), vals_c)
+                    tv = self._krylov_solve(lu, vals_c, e_l)
+                if tv is None:
+                    tv = lu.solve(e_l)
                 self.timers["solve"] += time.perf_counter() - ts
                 t_new = tv / np.linalg.norm(tv)
                 if np.dot(t_new, t) < 0.0:
