@@ -350,10 +350,9 @@ __global__ void k_gather_jacobian32(const GatherArgs g, const float *__restrict_
     const int r = (int)(t - (int64_t)blk * 36);
     const int jeq = r / 6, ieq = r - 6 * (r / 6);
     const int64_t slot = g.rowptr[(int64_t)g.brow[blk] * 6 + jeq] + g.boff[blk] + ieq;
-    float acc = g.store ? 0.0f : vals[slot];
-    const int c0 = g.bptr[blk], c1 = g.bptr[blk + 1];
-    for (int c = c0; c < c1; c++) acc = acc + es[(int64_t)g.bcon[c] * 36 + r];
-    vals[slot] = acc;
+    const float acc0 = g.store ? 0.0f : vals[slot];
+    vals[slot] = ordered_sum(acc0, g.bcon, g.bptr[blk], g.bptr[blk + 1],
+                             [&](int c) { return es[(int64_t)c * 36 + r]; });
 }
 
 __global__ void k_gather_arclength32(const GatherArgs g, const float *__restrict__ as,
@@ -363,10 +362,9 @@ __global__ void k_gather_arclength32(const GatherArgs g, const float *__restrict
     if (t >= (int64_t)g.nnodes * 6) return;
     const int node = (int)(t / 6), jeq = (int)(t - (int64_t)node * 6);
     const int64_t slot = g.rowptr[t + 1] - 1;
-    float acc = g.store ? 0.0f : vals[slot];
-    const int c0 = g.nptr[node], c1 = g.nptr[node + 1];
-    for (int c = c0; c < c1; c++) acc = acc + as[(int64_t)g.ncon[c] * 6 + jeq];
-    vals[slot] = acc;
+    const float acc0 = g.store ? 0.0f : vals[slot];
+    vals[slot] = ordered_sum(acc0, g.ncon, g.nptr[node], g.nptr[node + 1],
+                             [&](int c) { return as[(int64_t)c * 6 + jeq]; });
 }
 
 cudaError_t launch_gather_jacobian32(const GatherArgs &g, const float *es, float *vals,

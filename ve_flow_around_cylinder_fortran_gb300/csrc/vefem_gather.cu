@@ -23,10 +23,9 @@ __global__ void k_gather_residual(const GatherArgs g, const double *__restrict__
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (int64_t)g.nnodes * 6) return;
     const int node = (int)(t / 6), jeq = (int)(t - (int64_t)node * 6);
-    double acc = g.store ? 0.0 : b[t];
-    const int c0 = g.nptr[node], c1 = g.nptr[node + 1];
-    for (int c = c0; c < c1; c++) acc = acc + rs[(int64_t)g.ncon[c] * 6 + jeq];
-    b[t] = acc;
+    const double acc0 = g.store ? 0.0 : b[t];
+    b[t] = ordered_sum(acc0, g.ncon, g.nptr[node], g.nptr[node + 1],
+                       [&](int c) { return rs[(int64_t)c * 6 + jeq]; });
 }
 
 // one thread per (node-pair block, jeq, ieq)
@@ -39,10 +38,9 @@ __global__ void k_gather_jacobian(const GatherArgs g, const double *__restrict__
     const int r = (int)(t - (int64_t)blk * 36);
     const int jeq = r / 6, ieq = r - 6 * (r / 6);
     const int64_t slot = g.rowptr[(int64_t)g.brow[blk] * 6 + jeq] + g.boff[blk] + ieq;
-    double acc = g.store ? 0.0 : vals[slot];
-    const int c0 = g.bptr[blk], c1 = g.bptr[blk + 1];
-    for (int c = c0; c < c1; c++) acc = acc + es[(int64_t)g.bcon[c] * 36 + r];
-    vals[slot] = acc;
+    const double acc0 = g.store ? 0.0 : vals[slot];
+    vals[slot] = ordered_sum(acc0, g.bcon, g.bptr[blk], g.bptr[blk + 1],
+                             [&](int c) { return es[(int64_t)c * 36 + r]; });
 }
 
 // arclength column: the last entry of every node row (column N - 1)
@@ -53,10 +51,9 @@ __global__ void k_gather_arclength(const GatherArgs g, const double *__restrict_
     if (t >= (int64_t)g.nnodes * 6) return;
     const int node = (int)(t / 6), jeq = (int)(t - (int64_t)node * 6);
     const int64_t slot = g.rowptr[t + 1] - 1;
-    double acc = g.store ? 0.0 : vals[slot];
-    const int c0 = g.nptr[node], c1 = g.nptr[node + 1];
-    for (int c = c0; c < c1; c++) acc = acc + as[(int64_t)g.ncon[c] * 6 + jeq];
-    vals[slot] = acc;
+    const double acc0 = g.store ? 0.0 : vals[slot];
+    vals[slot] = ordered_sum(acc0, g.ncon, g.nptr[node], g.nptr[node + 1],
+                             [&](int c) { return as[(int64_t)c * 6 + jeq]; });
 }
 
 // Dirichlet rows: b = TL - value, and the AIJ row zeroed with 1 on the diagonal

@@ -82,6 +82,30 @@ struct GatherArgs {
     int store = 0;             // 1: the sums start from zero (VEFEM_ZERO_FIRST), the
                                // destination is written without being read
 };
+#ifdef __CUDACC__
+// acc + val(con[c0]) + val(con[c0+1]) + ... in contributor order, the same
+// sum as the plain loop, but the first ORDERED_PREFETCH contributor ids, then
+// their values, are loaded before the first addition: independent loads in
+// flight instead of an id -> value -> add chain per contributor.
+constexpr int ORDERED_PREFETCH = 4;
+template <class T, class F>
+__device__ __forceinline__ T ordered_sum(T acc, const int32_t *__restrict__ con, int c0, int c1,
+                                         F val)
+{
+    int id[ORDERED_PREFETCH];
+    T v[ORDERED_PREFETCH];
+#pragma unroll
+    for (int k = 0; k < ORDERED_PREFETCH; k++) id[k] = c0 + k < c1 ? con[c0 + k] : 0;
+#pragma unroll
+    for (int k = 0; k < ORDERED_PREFETCH; k++) v[k] = c0 + k < c1 ? val(id[k]) : T(0);
+#pragma unroll
+    for (int k = 0; k < ORDERED_PREFETCH; k++)
+        if (c0 + k < c1) acc = acc + v[k];
+    for (int c = c0 + ORDERED_PREFETCH; c < c1; c++) acc = acc + val(con[c]);
+    return acc;
+}
+#endif
+
 cudaError_t launch_gather_residual(const GatherArgs &g, const double *rs, double *b,
                                    cudaStream_t s);
 cudaError_t launch_gather_jacobian(const GatherArgs &g, const double *es, double *vals,
