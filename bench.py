@@ -490,12 +490,13 @@ def newton_precision_compare(nel: int, device: int = 0, wis=(0.1, 0.2, 0.3, 0.4,
     # shared solver with delayed pressures (larger fronts) for the rest
     for jac in ("exact32", "fd64"):
         t0 = time.perf_counter()
-        # a point whose Newton iteration diverges ends the run (no emergency
-        # restarts: relaxed Newton at this size takes minutes per attempt);
-        # the points before it are reported
+        # a point whose Newton iteration diverges, or has not converged after
+        # 20 iterations, ends the run (no emergency restarts: relaxed Newton
+        # at this size takes minutes per attempt); the points before it are
+        # reported
         res = NW.natural_continuation(asm, mesh, phys, list(wis), jacobian=jac, tol=1e-10,
                                       linear_solver=solver, max_restarts=0,
-                                      stop_on_failure=True)
+                                      stop_on_failure=True, max_iter=20)
         wall = time.perf_counter() - t0
         runs[jac] = {
             "wall_s": wall,

@@ -254,12 +254,14 @@ def extrapolate(wis_done, TLs, wi: float) -> np.ndarray:
 def natural_continuation(asm, mesh, phys: S.Physics, wis, jacobian: str = "fd64",
                          tol: float = 1.0e-10, outlet_edges: bool = True, TL=None, log=None,
                          linear_solver="superlu", predictor: bool = True,
-                         max_restarts=None, stop_on_failure: bool = False):
+                         max_restarts=None, stop_on_failure: bool = False,
+                         max_iter: int = NITER):
     """Solve at each Weissenberg number of ``wis`` in turn (the inflow
     Dirichlet data follow Wi), each from the previous solution or, with
     ``predictor``, from the extrapolation through the last converged
-    solutions (``extrapolate``).  ``max_restarts`` bounds the emergency
-    restarts per point; a point that does not converge raises, or with
+    solutions (``extrapolate``).  ``max_iter`` bounds the Newton iterations
+    of a first attempt (Niter), ``max_restarts`` the emergency restarts per
+    point; a point that does not converge raises, or with
     ``stop_on_failure`` ends the run.  Returns the list of NewtonResult of
     the converged points."""
     out = []
@@ -279,7 +281,8 @@ def natural_continuation(asm, mesh, phys: S.Physics, wis, jacobian: str = "fd64"
         nr = NewtonRaphson(DeviceAssembly(asm, rows, values, jacobian, outlet_edges),
                            asm.rowptr, asm.colind, p.nex, mesh, linear_solver=solver)
         try:
-            res = emergency_solve(nr, TL, EU, log=log, tol=tol, max_restarts=max_restarts)
+            res = emergency_solve(nr, TL, EU, log=log, tol=tol, max_restarts=max_restarts,
+                                  max_iter=max_iter)
         except (RuntimeError, FloatingPointError):
             if not stop_on_failure:
                 raise
