@@ -214,7 +214,8 @@ int vefem_abi_version(void);
  * q (device, int64); ext [ext_off[q] ..) the position in panel q+1 of each
  * front unknown of panel q (device, int32).  Every unknown is a pivot of
  * exactly one panel (the p[q] sum to N).  The device arrays are the caller's
- * and must outlive the handle.
+ * and must outlive the handle; create reads idx once, synchronously, to set up
+ * the solve's elimination order (N and the entries of idx below 2^31).
  * vefem_frontal_factor: buf holds the assembled original entries of every
  * panel (zeros elsewhere); the elimination (blocked Gauss-Jordan without
  * pivoting, with the Schur complement of each panel added into the next one)
