@@ -96,3 +96,29 @@ def test_zero_pivot_falls_back_to_host():
     x = lu.solve(b)
     assert lu.fallbacks == 1
     assert np.linalg.norm(A @ x - b) <= 1e-10 * np.linalg.norm(b)
+
+
+def test_krylov_correction_with_device_tensors():
+    """The Newton-Krylov correction of the continuation driver on device
+    tensors (torch's CPU device here): GMRES with the Jacobian as a torch CSR
+    matrix, preconditioned by the frontal factorisation of a perturbed
+    matrix (an older Jacobian), solves to its tolerance; the preconditioner
+    alone does not."""
+    import types
+
+    from ve_flow_around_cylinder_fortran_gb300 import continuation as C
+    mesh, rp, ci, v, b, A = _bordered(200, 1)
+    old = v * (1.0 + 0.02 * np.random.default_rng(3).standard_normal(len(v)))
+    lu = FR.FrontalLU(rp, ci, mesh, device="cpu").factor(old)
+    cont = types.SimpleNamespace(cfg=C.ArclengthSettings(krylov=20, krylov_rtol=1e-8),
+                                 lrow=types.SimpleNamespace(rowptr=rp, colind=ci),
+                                 N=len(rp) - 1, krylov_iterations=0, krylov_failures=0,
+                                 last_krylov_its=0)
+    s = C.ArclengthContinuation._krylov_solve(cont, lu, torch.from_numpy(v), b)
+    assert s is not None and cont.krylov_iterations > 1
+    assert np.linalg.norm(A @ s - b) <= 1e-7 * np.linalg.norm(b)
+    assert np.linalg.norm(A @ lu.solve(b) - b) > 1e-4 * np.linalg.norm(b)
+    # a tolerance GMRES cannot reach in the iterations allowed: no correction
+    cont.cfg = C.ArclengthSettings(krylov=1, krylov_rtol=1e-14)
+    assert C.ArclengthContinuation._krylov_solve(cont, lu, torch.from_numpy(v), b) is None
+    assert cont.krylov_failures == 1
